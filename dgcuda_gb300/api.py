@@ -1,0 +1,297 @@
+"""ctypes binding of include/dg.h (see the package docstring)."""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+ADVECTION, EULER, SHALLOW_WATER, MAXWELL = 0, 1, 2, 3
+SSP_RK3, RK4, RK2 = 0, 1, 2
+BC_REFLECT, BC_OUTFLOW, BC_INFLOW, BC_TRANSMISSIVE, PERIODIC = -1, -2, -3, -4, 0
+PROBLEMS = {
+    "none": 0, "adv_sine": 1, "adv_linear": 2, "euler_vortex": 3, "euler_riemann4": 4,
+    "euler_supersonic": 5, "sw_hump": 6, "sw_test": 7, "maxwell_plane": 8,
+}
+_NVARS = {ADVECTION: 1, EULER: 4, SHALLOW_WATER: 3, MAXWELL: 3}
+_STATUS = ["OK", "BAD_ARG", "BAD_MESH", "NONPHYSICAL", "NAN", "CUDA_ERROR", "TIMEOUT",
+           "IO_ERROR", "UNSUPPORTED"]
+
+
+def n_modes(p):
+    return (p + 1) * (p + 2) // 2
+
+
+def n_vars(eq):
+    return _NVARS[eq]
+
+
+class DGError(RuntimeError):
+    def __init__(self, status, msg):
+        self.status = status
+        name = _STATUS[status] if 0 <= status < len(_STATUS) else str(status)
+        super().__init__("%s: %s" % (name, msg))
+
+
+class Params(C.Structure):
+    _fields_ = [("gamma", C.c_double), ("gravity", C.c_double), ("ax", C.c_double),
+                ("ay", C.c_double), ("mu", C.c_double), ("eps", C.c_double),
+                ("problem", C.c_int), ("limiter", C.c_int), ("cfl", C.c_double),
+                ("prm", C.c_double * 8)]
+
+
+def lib_path():
+    return os.path.join(HERE, "libdg_gb300.so")
+
+
+_LIB = None
+
+
+def load_library():
+    """Load libdg_gb300.so; raises when it has not been built."""
+    global _LIB
+    if _LIB is None:
+        path = lib_path()
+        if not os.path.exists(path):
+            raise ImportError("libdg_gb300.so not built: run "
+                              "`python -c 'import __graft_entry__ as g; g.build()'`")
+        _LIB = C.CDLL(path)
+        _declare(_LIB)
+    return _LIB
+
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+def _declare(L):
+    sigs = {
+        "dg_version": (C.c_char_p, []),
+        "dg_last_error": (C.c_char_p, []),
+        "dg_params_default": (None, [C.POINTER(Params)]),
+        "dg_mesh_read_pmsh": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
+        "dg_mesh_write_pmsh": (C.c_int, [C.c_void_p, C.c_char_p]),
+        "dg_mesh_from_arrays": (C.c_int, [C.c_int, _dp, _ip, C.c_int, _dp, _ip,
+                                          C.POINTER(C.c_void_p)]),
+        "dg_mesh_get_arrays": (C.c_int, [C.c_void_p, _dp, _ip, _dp, _ip]),
+        "dg_mesh_sizes": (C.c_int, [C.c_void_p, _ip, _ip]),
+        "dg_mesh_square": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                     C.c_double, C.c_double, C.c_uint64, _ip,
+                                     C.POINTER(C.c_void_p)]),
+        "dg_mesh_destroy": (None, [C.c_void_p]),
+        "dg_solver_create": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(Params), C.c_int,
+                                       C.POINTER(C.c_void_p)]),
+        "dg_solver_destroy": (None, [C.c_void_p]),
+        "dg_solver_sizes": (C.c_int, [C.c_void_p, _ip, _ip, _ip, _ip]),
+        "dg_solver_stream": (C.c_void_p, [C.c_void_p]),
+        "dg_solver_set_tables": (C.c_int, [C.c_void_p, C.c_int, C.c_int] + [_dp] * 10),
+        "dg_init": (C.c_int, [C.c_void_p]),
+        "dg_set_state": (C.c_int, [C.c_void_p, _dp]),
+        "dg_get_state": (C.c_int, [C.c_void_p, _dp]),
+        "dg_set_state_device": (C.c_int, [C.c_void_p, C.c_void_p]),
+        "dg_get_state_device": (C.c_int, [C.c_void_p, C.c_void_p]),
+        "dg_rhs": (C.c_int, [C.c_void_p, C.c_double, _dp, _dp]),
+        "dg_limit": (C.c_int, [C.c_void_p]),
+        "dg_step": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, _dp]),
+        "dg_advance_to": (C.c_int, [C.c_void_p, C.c_double, C.c_int, _dp, _ip]),
+        "dg_cfl": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
+        "dg_l2_error": (C.c_int, [C.c_void_p, C.c_double, _dp]),
+        "dg_profile_enable": (C.c_int, [C.c_void_p, C.c_int]),
+        "dg_profile_get": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_longlong), _dp]),
+        "dg_profile_reset": (C.c_int, [C.c_void_p]),
+        "dg_kernel_launches": (C.c_longlong, [C.c_void_p]),
+    }
+    for name, (res, args) in sigs.items():
+        fn = getattr(L, name, None)
+        if fn is None:
+            continue
+        fn.restype = res
+        fn.argtypes = args
+
+
+def _check(st):
+    if st != 0:
+        raise DGError(st, load_library().dg_last_error().decode())
+
+
+def _dptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _iptr(a):
+    return a.ctypes.data_as(_ip)
+
+
+class Mesh:
+    """A .pmsh triangle mesh (host object)."""
+
+    def __init__(self, handle):
+        self._h = C.c_void_p(handle) if not isinstance(handle, C.c_void_p) else handle
+        self._L = load_library()
+        K, S = C.c_int(), C.c_int()
+        _check(self._L.dg_mesh_sizes(self._h, C.byref(K), C.byref(S)))
+        self.K, self.S = K.value, S.value
+
+    @classmethod
+    def read_mesh(cls, path):
+        """Read a .pmsh file (main.cu:205-277)."""
+        L = load_library()
+        h = C.c_void_p()
+        _check(L.dg_mesh_read_pmsh(os.fsencode(path), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def square(cls, nx, ny, box=(0.0, 1.0, 0.0, 1.0), jitter=0.0, seed=0,
+               bc=(PERIODIC, PERIODIC, PERIODIC, PERIODIC)):
+        L = load_library()
+        h = C.c_void_p()
+        b = np.asarray(bc, dtype=np.int32)
+        _check(L.dg_mesh_square(nx, ny, box[0], box[1], box[2], box[3], jitter, seed, _iptr(b),
+                                C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_arrays(cls, V, elem_sides, side_xy, side_elems):
+        L = load_library()
+        V = np.ascontiguousarray(V, dtype=np.float64)
+        es = np.ascontiguousarray(elem_sides, dtype=np.int32)
+        sxy = np.ascontiguousarray(side_xy, dtype=np.float64)
+        se = np.ascontiguousarray(side_elems, dtype=np.int32)
+        K, S = V.shape[-1], sxy.shape[-1]
+        h = C.c_void_p()
+        _check(L.dg_mesh_from_arrays(K, _dptr(V), _iptr(es), S, _dptr(sxy), _iptr(se),
+                                     C.byref(h)))
+        return cls(h)
+
+    def arrays(self):
+        """(V[6,K], elem_sides[3,K], side_xy[4,S], side_elems[4,S]) in .pmsh column order."""
+        V = np.empty((6, self.K))
+        es = np.empty((3, self.K), dtype=np.int32)
+        sxy = np.empty((4, self.S))
+        se = np.empty((4, self.S), dtype=np.int32)
+        _check(self._L.dg_mesh_get_arrays(self._h, _dptr(V), _iptr(es), _dptr(sxy), _iptr(se)))
+        return V, es, sxy, se
+
+    def write(self, path):
+        _check(self._L.dg_mesh_write_pmsh(self._h, os.fsencode(path)))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._L.dg_mesh_destroy(h)
+            self._h = None
+
+
+class Solver:
+    """One RK-DG problem on one GPU (wraps dg_solver)."""
+
+    def __init__(self, mesh, eq, p, params=None, device=0, **kw):
+        self._L = load_library()
+        prm = Params()
+        self._L.dg_params_default(C.byref(prm))
+        if params is not None:
+            prm = params
+        for k, v in kw.items():
+            if k == "problem" and isinstance(v, str):
+                v = PROBLEMS[v]
+            if k == "prm":
+                for i, x in enumerate(v):
+                    prm.prm[i] = x
+                continue
+            setattr(prm, k, v)
+        self.params = prm
+        self.mesh = mesh
+        h = C.c_void_p()
+        _check(self._L.dg_solver_create(mesh._h, eq, p, C.byref(prm), device, C.byref(h)))
+        self._h = h
+        N, npm, K, S = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        _check(self._L.dg_solver_sizes(h, C.byref(N), C.byref(npm), C.byref(K), C.byref(S)))
+        self.N, self.n_p, self.K, self.S = N.value, npm.value, K.value, S.value
+        self.eq, self.p = eq, p
+
+    @property
+    def shape(self):
+        return (self.N, self.n_p, self.K)
+
+    def set_tables(self, basis, grad_x, grad_y, side, vertex, w, r1, r2, r_oned, w_oned):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in
+                (basis, grad_x, grad_y, side, vertex, w, r1, r2, r_oned, w_oned)]
+        _check(self._L.dg_solver_set_tables(self._h, len(arrs[5]), len(arrs[8]),
+                                            *[_dptr(a) for a in arrs]))
+
+    def init_conditions(self):
+        _check(self._L.dg_init(self._h))
+
+    def set_state(self, c):
+        c = np.ascontiguousarray(c, dtype=np.float64).reshape(self.shape)
+        _check(self._L.dg_set_state(self._h, _dptr(c)))
+
+    def get_state(self):
+        c = np.empty(self.shape)
+        _check(self._L.dg_get_state(self._h, _dptr(c)))
+        return c
+
+    def eval_rhs(self, c, t=0.0):
+        c = np.ascontiguousarray(c, dtype=np.float64).reshape(self.shape)
+        out = np.empty(self.shape)
+        _check(self._L.dg_rhs(self._h, t, _dptr(c), _dptr(out)))
+        return out
+
+    def limit_c(self):
+        _check(self._L.dg_limit(self._h))
+
+    def step(self, nsteps, scheme=SSP_RK3, t=0.0, dt=0.0):
+        tt = C.c_double(t)
+        _check(self._L.dg_step(self._h, nsteps, scheme, dt, C.byref(tt)))
+        return tt.value
+
+    def advance_to(self, T, scheme=SSP_RK3, t=0.0):
+        tt, n = C.c_double(t), C.c_int()
+        _check(self._L.dg_advance_to(self._h, T, scheme, C.byref(tt), C.byref(n)))
+        return tt.value, n.value
+
+    def time_integrate_rk4(self, nsteps, t=0.0):
+        return self.step(nsteps, RK4, t)
+
+    def time_integrate_rk2(self, nsteps, t=0.0):
+        return self.step(nsteps, RK2, t)
+
+    def time_integrate_ssp_rk3(self, nsteps, t=0.0):
+        return self.step(nsteps, SSP_RK3, t)
+
+    def cfl(self):
+        dt, lam, dmin = C.c_double(), C.c_double(), C.c_double()
+        _check(self._L.dg_cfl(self._h, C.byref(dt), C.byref(lam), C.byref(dmin)))
+        return dt.value, lam.value, dmin.value
+
+    def eval_error_L2(self, t):
+        err = np.empty(self.N)
+        _check(self._L.dg_l2_error(self._h, t, _dptr(err)))
+        return err
+
+    def stream(self):
+        return self._L.dg_solver_stream(self._h)
+
+    def profile(self, on=True):
+        _check(self._L.dg_profile_enable(self._h, 1 if on else 0))
+
+    def profile_reset(self):
+        _check(self._L.dg_profile_reset(self._h))
+
+    def profile_get(self, kernel):
+        n, ms = C.c_longlong(), C.c_double()
+        _check(self._L.dg_profile_get(self._h, kernel.encode(), C.byref(n), C.byref(ms)))
+        return n.value, ms.value
+
+    def kernel_launches(self):
+        return self._L.dg_kernel_launches(self._h)
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._L.dg_solver_destroy(h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+

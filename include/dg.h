@@ -1,0 +1,177 @@
+/* dg.h -- C ABI of the GB300 RK-DG solver (dgcuda_gb300).
+ *
+ * A drop-in for the RK-DG hot path of DGCUDA (src/2d/conservation): read a
+ * .pmsh triangle mesh, pick an equation module and order p, project the
+ * initial condition, evaluate the DG right-hand side, step with SSP-RK3 (or
+ * the reference's RK4 / midpoint RK2) with the optional slope limiter, and
+ * measure the L2 error.  Every call returns a dg_status and never exits the
+ * process; dg_last_error() gives the message of the last failure on the
+ * calling thread.
+ *
+ * Data layout at the boundary is the reference's: a state array is
+ * C[var][mode][elem] (conserv_kernels.cu:224), elements and sides in .pmsh
+ * order.  Internally elements are renumbered along a space-filling curve;
+ * the permutation is applied at the boundary.
+ *
+ * All pointers are plain host pointers unless a name says _device.
+ */
+#ifndef DG_GB300_H
+#define DG_GB300_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  DG_OK = 0,
+  DG_BAD_ARG = 1,
+  DG_BAD_MESH = 2,     /* replaces read_mesh's printf + exit (main.cu:242-245, 272-275) */
+  DG_NONPHYSICAL = 3,
+  DG_NAN = 4,          /* replaces the NaN-dt early return (time_integrator.cu:219-223) */
+  DG_CUDA_ERROR = 5,   /* replaces checkCudaError's exit(-1) (main.cu:196-203) */
+  DG_TIMEOUT = 6,
+  DG_IO_ERROR = 7,
+  DG_UNSUPPORTED = 8
+} dg_status;
+
+/* equation modules (src/2d/conservation/{advection,euler,shallowwater,maxwells}) */
+typedef enum { DG_ADVECTION = 0, DG_EULER = 1, DG_SHALLOW_WATER = 2, DG_MAXWELL = 3 } dg_equation;
+
+/* time integrators: the reference's RK4 = 1 and RK2 = 2 (main.cu:35-36), plus SSP-RK3 */
+typedef enum { DG_SSP_RK3 = 0, DG_RK4 = 1, DG_RK2 = 2 } dg_scheme;
+
+/* problem plugins: initial condition, boundary ghost states and exact
+ * solution (the reference's per-problem U0 / U_inflow / U_outflow /
+ * U_reflection / U_exact device functions, e.g. supersonic.cu:27-97) */
+typedef enum {
+  DG_PB_NONE = 0,           /* state set by the caller; ghost states zero */
+  DG_PB_ADV_SINE = 1,       /* u0 = sin(2 pi x) sin(2 pi y), exact = translated */
+  DG_PB_ADV_LINEAR = 2,     /* u0 = x - y (advection/exact/exact.cu) */
+  DG_PB_EULER_VORTEX = 3,   /* isentropic vortex: prm beta, x0, y0, uinf, vinf, L */
+  DG_PB_EULER_RIEMANN4 = 4, /* four-quadrant Riemann problem on [0,1]^2 */
+  DG_PB_EULER_SUPERSONIC = 5, /* supersonic vortex (euler/supersonic/supersonic.cu) */
+  DG_PB_SW_HUMP = 6,        /* still water hump: prm h0, A, sigma, x0, y0 */
+  DG_PB_SW_TEST = 7,        /* shallowwater/test/test.cu hump */
+  DG_PB_MAXWELL_PLANE = 8   /* plane TM wave along x */
+} dg_problem;
+
+/* boundary codes in the .pmsh right-element column (genmesh.py:166-174) */
+#define DG_BC_REFLECT (-1)
+#define DG_BC_OUTFLOW (-2)
+#define DG_BC_INFLOW (-3)
+#define DG_BC_TRANSMISSIVE (-4) /* new: ghost = interior trace */
+
+typedef struct {
+  double gamma;   /* Euler ratio of specific heats (get_GAMMA, supersonic.cu:105) */
+  double gravity; /* shallow water g (the reference hard-codes 9.8, shallowwater.cu:7) */
+  double ax, ay;  /* advection velocity (get_velocity, exact.cu:34-37) */
+  double mu, eps; /* Maxwell material constants (get_mu/get_eps, cmirror.cu) */
+  int problem;    /* dg_problem */
+  int limiter;    /* 1 = Barth-Jespersen limiter (limit_c, conserv_kernels.cu:640) */
+  double cfl;     /* dt = cfl * d_min / lambda_max / (2p + 1) (time_integrator.cu:217) */
+  double prm[8];  /* problem parameters, see dg_problem */
+} dg_params;
+
+typedef struct dg_mesh dg_mesh;
+typedef struct dg_solver dg_solver;
+
+const char *dg_version(void);
+const char *dg_last_error(void);
+/* fills *p with the defaults: gamma 1.4, g 9.81, a = (1, 0.5), mu = eps = 1,
+ * cfl 0.3, limiter off, problem DG_PB_NONE */
+void dg_params_default(dg_params *p);
+
+/* ---- meshes (host only; no GPU needed) ---------------------------------
+ * replaces read_mesh (main.cu:205-277) and genmesh.py's .pmsh writer
+ * (genmesh.py:286-313) */
+dg_status dg_mesh_read_pmsh(const char *path, dg_mesh **out);
+dg_status dg_mesh_write_pmsh(const dg_mesh *m, const char *path);
+/* arrays in .pmsh column order: V = 6*K doubles as V1x[K],V1y[K],V2x[K],
+ * V2y[K],V3x[K],V3y[K]; elem_sides = 3*K ints s1[K],s2[K],s3[K];
+ * side_xy = 4*S doubles x1[S],y1[S],x2[S],y2[S]; side_elems = 4*S ints
+ * left[S],right[S],left_side[S],right_side[S] */
+dg_status dg_mesh_from_arrays(int K, const double *V, const int *elem_sides, int S,
+                              const double *side_xy, const int *side_elems, dg_mesh **out);
+dg_status dg_mesh_get_arrays(const dg_mesh *m, double *V, int *elem_sides, double *side_xy,
+                             int *side_elems);
+dg_status dg_mesh_sizes(const dg_mesh *m, int *K, int *S);
+/* nx x ny squares on [x0,x1]x[y0,y1], each cut along the (0,0)-(1,1)
+ * diagonal into two CCW triangles; interior vertices jittered uniformly by
+ * +-jitter*h (splitmix64, seed).  bc = {left, right, bottom, top}: 0 means
+ * periodic (both sides of a pair must be 0), else a DG_BC_* code. */
+dg_status dg_mesh_square(int nx, int ny, double x0, double x1, double y0, double y1,
+                         double jitter, uint64_t seed, const int bc[4], dg_mesh **out);
+void dg_mesh_destroy(dg_mesh *m);
+
+/* ---- solver -------------------------------------------------------------
+ * replaces run_dgcuda's set-up (init_gpu, set_quadrature, preval_* and
+ * preval_basis; main.cu:600-806).  p = 0..5.  device = CUDA ordinal. */
+dg_status dg_solver_create(const dg_mesh *m, dg_equation eq, int p, const dg_params *prm,
+                           int device, dg_solver **out);
+void dg_solver_destroy(dg_solver *s);
+/* number of variables N and modes n_p */
+dg_status dg_solver_sizes(const dg_solver *s, int *N, int *n_p, int *K, int *S);
+/* the CUDA stream all work is issued on (a cudaStream_t) */
+void *dg_solver_stream(dg_solver *s);
+
+/* Override the basis / quadrature tabulation with the caller's, in the
+ * reference's constant-table layouts (conserv_kernels.cu:42-76,
+ * basis.cu:196-214): basis[i*n_q+j], grad_x/grad_y[i*n_q+j] (weights
+ * folded in), side[f*n_p*n_1 + i*n_1 + j], vertex[i*3+v], w[n_q],
+ * r1[n_q], r2[n_q], r_oned[n_1], w_oned[n_1].  n_q, n_1 must match p. */
+dg_status dg_solver_set_tables(dg_solver *s, int n_q, int n_1, const double *basis,
+                               const double *grad_x, const double *grad_y, const double *side,
+                               const double *vertex, const double *w, const double *r1,
+                               const double *r2, const double *r_oned, const double *w_oned);
+
+/* L2 projection of the problem's initial condition (init_conditions,
+ * conserv_kernels.cu:201-228) */
+dg_status dg_init(dg_solver *s);
+/* state copy in / out, reference layout C[var][mode][elem], .pmsh order */
+dg_status dg_set_state(dg_solver *s, const double *C);
+dg_status dg_get_state(dg_solver *s, double *C);
+/* same, with device pointers (no host staging) */
+dg_status dg_set_state_device(dg_solver *s, const double *C_device);
+dg_status dg_get_state_device(dg_solver *s, double *C_device);
+
+/* du/dt of the DG operator at time t for state C (host arrays, reference
+ * layout): eval_surface + eval_volume + eval_rhs with dt = 1
+ * (conserv_kernels.cu:899-1083, time_integrator.cu:26-101) */
+dg_status dg_rhs(dg_solver *s, double t, const double *C, double *dCdt);
+
+/* apply the slope limiter to the current state (limit_c) */
+dg_status dg_limit(dg_solver *s);
+
+/* nsteps time steps of `scheme` from the current state; each step takes
+ * dt from the CFL condition on the device (eval_global_lambda + max,
+ * time_integrator.cu:200-217) unless fixed_dt > 0.  *t is read and
+ * advanced. */
+dg_status dg_step(dg_solver *s, int nsteps, dg_scheme scheme, double fixed_dt, double *t);
+/* step until t == T (the last step is shortened to land on T). */
+dg_status dg_advance_to(dg_solver *s, double T, dg_scheme scheme, double *t, int *nsteps);
+
+/* current CFL time step and the quantities it is built from */
+dg_status dg_cfl(dg_solver *s, double *dt, double *lambda_max, double *d_min);
+
+/* per-variable L2 error against the problem's exact solution at time t:
+ * err[n] = sqrt(sum_e int_e (u_n - u_exact,n)^2) (eval_error_L2 + host sum,
+ * conserv_kernels.cu:1432-1479, main.cu:859-875) */
+dg_status dg_l2_error(dg_solver *s, double t, double *err);
+
+/* Timing of the solver's own kernels (CUDA events around each launch on the
+ * solver stream).  When enabled, dg_step launches kernels directly instead
+ * of replaying a CUDA graph. */
+dg_status dg_profile_enable(dg_solver *s, int on);
+/* names: "trace", "face", "element", "limit", "cfl"; fills launches and the
+ * summed milliseconds since the last reset */
+dg_status dg_profile_get(dg_solver *s, const char *kernel, long long *launches, double *ms);
+dg_status dg_profile_reset(dg_solver *s);
+/* launches of the solver's kernels since creation (all kinds) */
+long long dg_kernel_launches(const dg_solver *s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
