@@ -1,0 +1,310 @@
+// dg_device.cuh -- equation modules, problem plugins and per-order tables
+// for the sm_103a kernels.
+//
+// Equation modules follow the reference's compile-time plugin contract
+// (src/2d/conservation/conserv_headers.cuh:5-34) as C++ traits: physical
+// flux (eval_flux), numerical flux (riemann_solver), admissibility
+// (is_physical), the CFL wave speed of a cell mean (eval_global_lambda) and
+// the boundary ghost state (eval_boundary + the problem's U_* functions).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "dg_tables_data.h"
+
+#define DG_HD __host__ __device__ __forceinline__
+
+namespace dg {
+
+constexpr int np_of(int p) { return (p + 1) * (p + 2) / 2; }
+constexpr int nq_of(int p) { return p == 0 ? 1 : p == 1 ? 3 : p == 2 ? 6 : p == 3 ? 12 : p == 4 ? 16 : 25; }
+
+// Per-order tabulation passed to every kernel as a __grid_constant__
+// parameter: with the loops below fully unrolled every table entry is a
+// constant-bank operand of the FP64 FMA that uses it.
+template <int P>
+struct Tab {
+  static constexpr int NP = np_of(P), NQ = nq_of(P), N1 = P + 1;
+  double B[NQ][NP];      // phi_i at volume point q
+  double GR[NQ][NP];     // w_q dphi_i/dr
+  double GS[NQ][NP];     // w_q dphi_i/ds
+  double E[3][N1][NP];   // phi_i at edge point j of face f (face 2 reversed)
+  double r[NQ], s[NQ], w[NQ];
+  double t1[N1], w1[N1];
+};
+
+// equation / problem parameters (kernel parameter)
+struct EqP {
+  double gamma, g, ax, ay, mu, eps;
+  int problem, pad;
+  double prm[8];
+};
+
+enum Problem {
+  PB_NONE = 0, PB_ADV_SINE = 1, PB_ADV_LINEAR = 2, PB_EULER_VORTEX = 3, PB_EULER_RIEMANN4 = 4,
+  PB_EULER_SUPERSONIC = 5, PB_SW_HUMP = 6, PB_SW_TEST = 7, PB_MAXWELL_PLANE = 8
+};
+
+constexpr double kPi = 3.141592653589793238462643383279502884;
+
+// --------------------------------------------------------------------------
+// problem plugins: exact / initial / inflow state (U0, U_exact, U_inflow)
+// --------------------------------------------------------------------------
+DG_HD void exact_state(const EqP &q, double *U, double x, double y, double t) {
+  const double *P = q.prm;
+  switch (q.problem) {
+    case PB_ADV_SINE: {
+      double xs = x - q.ax * t, ys = y - q.ay * t;
+      U[0] = sin(2 * kPi * xs) * sin(2 * kPi * ys);
+      break;
+    }
+    case PB_ADV_LINEAR:  // advection/exact/exact.cu:25-27
+      U[0] = x - y;
+      break;
+    case PB_EULER_VORTEX: {  // isentropic vortex, centre advected with (uinf, vinf)
+      double gam = q.gamma, beta = P[0], L = P[5];
+      double dx = x - (P[1] + P[3] * t), dy = y - (P[2] + P[4] * t);
+      if (L > 0) {
+        dx -= L * floor(dx / L + 0.5);
+        dy -= L * floor(dy / L + 0.5);
+      }
+      double r2 = dx * dx + dy * dy;
+      double e = exp(0.5 * (1 - r2));
+      double u = P[3] - beta / (2 * kPi) * e * dy;
+      double v = P[4] + beta / (2 * kPi) * e * dx;
+      double T = 1 - (gam - 1) * beta * beta / (8 * gam * kPi * kPi) * e * e;
+      double rho = pow(T, 1 / (gam - 1));
+      double p = pow(rho, gam);
+      U[0] = rho;
+      U[1] = rho * u;
+      U[2] = rho * v;
+      U[3] = p / (gam - 1) + 0.5 * rho * (u * u + v * v);
+      break;
+    }
+    case PB_EULER_RIEMANN4: {  // four-quadrant Riemann data split at (0.5, 0.5)
+      double gam = q.gamma, rho, u, v, p;
+      if (x >= 0.5 && y >= 0.5) { rho = 1.5; u = 0; v = 0; p = 1.5; }
+      else if (x < 0.5 && y >= 0.5) { rho = 0.5323; u = 1.206; v = 0; p = 0.3; }
+      else if (x < 0.5 && y < 0.5) { rho = 0.138; u = 1.206; v = 1.206; p = 0.029; }
+      else { rho = 0.5323; u = 0; v = 1.206; p = 0.3; }
+      U[0] = rho;
+      U[1] = rho * u;
+      U[2] = rho * v;
+      U[3] = p / (gam - 1) + 0.5 * rho * (u * u + v * v);
+      break;
+    }
+    case PB_EULER_SUPERSONIC: {  // euler/supersonic/supersonic.cu:27-37
+      const double GAM = 1.4, MACH = 2.25;
+      double r = sqrt(x * x + y * y);
+      U[0] = pow(1 + 1.0125 * (1. - 1. / (r * r)), 2.5);
+      U[1] = U[0] * sin(atan(y / x)) * MACH / r;
+      U[2] = U[0] * -cos(atan(y / x)) * MACH / r;
+      double p = (1.0 / GAM) * pow(U[0], GAM);
+      U[3] = 0.5 * U[0] * (MACH * MACH / (r * r)) + p * (1. / (GAM - 1.));
+      break;
+    }
+    case PB_SW_HUMP: {  // still water with a Gaussian hump: h0, A, sigma, x0, y0
+      double dx = x - P[3], dy = y - P[4], s = P[2];
+      U[0] = P[0] + P[1] * exp(-(dx * dx + dy * dy) / (s * s));
+      U[1] = 0;
+      U[2] = 0;
+      break;
+    }
+    case PB_SW_TEST:  // shallowwater/test/test.cu:25-35
+      U[0] = 10 + exp(-((x - 0.5) * (x - 0.5) + (y - 0.5) * (y - 0.5)) / (2 * 0.1 * 0.1));
+      U[1] = 0;
+      U[2] = 0;
+      break;
+    case PB_MAXWELL_PLANE: {  // plane TM wave along x
+      double c = 1 / sqrt(q.mu * q.eps);
+      double ez = sin(2 * kPi * (x - c * t));
+      U[0] = 0;
+      U[1] = sqrt(q.eps / q.mu) * ez;
+      U[2] = ez;
+      break;
+    }
+    default:
+      U[0] = U[1] = U[2] = U[3] = 0;
+  }
+}
+
+// --------------------------------------------------------------------------
+// equation modules
+// --------------------------------------------------------------------------
+struct Advection {  // advection/advection.cu
+  static constexpr int N = 1;
+  DG_HD static bool physical(const EqP &, const double *) { return true; }
+  DG_HD static void flux(const EqP &q, const double *U, double *fx, double *fy) {
+    fx[0] = q.ax * U[0];
+    fy[0] = q.ay * U[0];
+  }
+  // upwind flux (riemann_solver_upwind, advection.cu:94-116)
+  DG_HD static void riemann(const EqP &q, const double *UL, const double *UR, double nx, double ny,
+                            double *F) {
+    double an = nx * q.ax + ny * q.ay;
+    F[0] = an > 0 ? an * UL[0] : an * UR[0];
+  }
+  DG_HD static double mean_speed(const EqP &q, const double *) {
+    return sqrt(q.ax * q.ax + q.ay * q.ay);
+  }
+  DG_HD static void reflect(const EqP &, const double *, double *UR, double, double, double,
+                            double) {
+    UR[0] = 0;  // the reference's advection problems have no reflecting walls
+  }
+  static constexpr bool outflow_uses_exact = false;
+};
+
+struct Euler {  // euler/euler.cu
+  static constexpr int N = 4;
+  // rho >= 0 and p >= 0 (is_physical, euler.cu:76-86); with rho > 0,
+  // p < 0 <=> 2 rho E < |rho u|^2, which needs no FP64 division
+  DG_HD static bool physical(const EqP &, const double *U) {
+    if (U[0] < 0) return false;
+    return !(2.0 * U[0] * U[3] < U[1] * U[1] + U[2] * U[2]);
+  }
+  DG_HD static void flux(const EqP &q, const double *U, double *fx, double *fy) {
+    double ir = 1.0 / U[0];
+    double u = U[1] * ir, v = U[2] * ir;
+    double p = (q.gamma - 1.) * (U[3] - 0.5 * (U[1] * u + U[2] * v));
+    double H = U[3] + p;
+    fx[0] = U[1];
+    fx[1] = U[1] * u + p;
+    fx[2] = U[2] * u;
+    fx[3] = H * u;
+    fy[0] = U[2];
+    fy[1] = U[1] * v;
+    fy[2] = U[2] * v + p;
+    fy[3] = H * v;
+  }
+  // local Lax-Friedrichs (euler.cu:170-237)
+  DG_HD static void riemann(const EqP &q, const double *UL, const double *UR, double nx, double ny,
+                            double *F) {
+    double irl = 1.0 / UL[0], irr = 1.0 / UR[0];
+    double ul = UL[1] * irl, vl = UL[2] * irl, ur = UR[1] * irr, vr = UR[2] * irr;
+    double pl = (q.gamma - 1.) * (UL[3] - 0.5 * (UL[1] * ul + UL[2] * vl));
+    double pr = (q.gamma - 1.) * (UR[3] - 0.5 * (UR[1] * ur + UR[2] * vr));
+    double snl = nx * ul + ny * vl, snr = nx * ur + ny * vr;
+    double cl = sqrt(q.gamma * pl * irl), cr = sqrt(q.gamma * pr * irr);
+    double lam = fmax(fabs(snl) + cl, fabs(snr) + cr);
+    double fl0 = UL[0] * snl, fr0 = UR[0] * snr;
+    F[0] = 0.5 * (fl0 + fr0 + lam * (UL[0] - UR[0]));
+    F[1] = 0.5 * (UL[1] * snl + pl * nx + UR[1] * snr + pr * nx + lam * (UL[1] - UR[1]));
+    F[2] = 0.5 * (UL[2] * snl + pl * ny + UR[2] * snr + pr * ny + lam * (UL[2] - UR[2]));
+    F[3] = 0.5 * ((UL[3] + pl) * snl + (UR[3] + pr) * snr + lam * (UL[3] - UR[3]));
+  }
+  DG_HD static double mean_speed(const EqP &q, const double *U) {  // euler.cu:248-277
+    double p = (q.gamma - 1.) * (U[3] - (U[1] * U[1] + U[2] * U[2]) / 2. / U[0]);
+    double c = sqrt(q.gamma * p / U[0]);
+    double s = sqrt(U[1] * U[1] + U[2] * U[2]) / U[0];
+    return s > 0 ? s + c : -s + c;
+  }
+  DG_HD static void reflect(const EqP &q, const double *UL, double *UR, double x, double y,
+                            double nx, double ny) {
+    if (q.problem == PB_EULER_SUPERSONIC) {  // supersonic.cu:65-87, curved wall
+      double d = sqrt(x * x + y * y), Nx = x / d, Ny = y / d;
+      if (Nx * nx + Ny * ny < 0) {
+        Nx = -Nx;
+        Ny = -Ny;
+      }
+      UR[0] = UL[0];
+      UR[3] = UL[3];
+      UR[1] = (UL[1] * Ny - UL[2] * Nx) * Ny;
+      UR[2] = -(UL[1] * Ny - UL[2] * Nx) * Nx;
+    } else {  // slip wall: mirror the momentum
+      double dot = UL[1] * nx + UL[2] * ny;
+      UR[0] = UL[0];
+      UR[1] = UL[1] - 2 * dot * nx;
+      UR[2] = UL[2] - 2 * dot * ny;
+      UR[3] = UL[3];
+    }
+  }
+  static constexpr bool outflow_uses_exact = true;
+};
+
+struct ShallowWater {  // shallowwater/shallowwater.cu (g is a parameter here)
+  static constexpr int N = 3;
+  DG_HD static bool physical(const EqP &, const double *U) { return U[0] >= 0.; }
+  DG_HD static void flux(const EqP &q, const double *U, double *fx, double *fy) {
+    double ih = 1.0 / U[0];
+    double u = U[1] * ih, v = U[2] * ih, hp = 0.5 * q.g * U[0] * U[0];
+    fx[0] = U[1];
+    fx[1] = U[1] * u + hp;
+    fx[2] = U[2] * u;
+    fy[0] = U[2];
+    fy[1] = U[1] * v;
+    fy[2] = U[2] * v + hp;
+  }
+  DG_HD static void riemann(const EqP &q, const double *UL, const double *UR, double nx, double ny,
+                            double *F) {  // shallowwater.cu:118-185
+    double ihl = 1.0 / UL[0], ihr = 1.0 / UR[0];
+    double snl = (nx * UL[1] + ny * UL[2]) * ihl, snr = (nx * UR[1] + ny * UR[2]) * ihr;
+    double cl = sqrt(UL[0] * q.g), cr = sqrt(UR[0] * q.g);
+    double lam = fmax(fabs(snl) + cl, fabs(snr) + cr);
+    double pl = 0.5 * q.g * UL[0] * UL[0], pr = 0.5 * q.g * UR[0] * UR[0];
+    F[0] = 0.5 * (UL[0] * snl + UR[0] * snr + lam * (UL[0] - UR[0]));
+    F[1] = 0.5 * (UL[1] * snl + pl * nx + UR[1] * snr + pr * nx + lam * (UL[1] - UR[1]));
+    F[2] = 0.5 * (UL[2] * snl + pl * ny + UR[2] * snr + pr * ny + lam * (UL[2] - UR[2]));
+  }
+  DG_HD static double mean_speed(const EqP &q, const double *U) {  // shallowwater.cu:196-224
+    double c = sqrt(U[0] * q.g);
+    double s = sqrt(U[1] * U[1] + U[2] * U[2]) / U[0];
+    return s > 0 ? s + c : -s + c;
+  }
+  DG_HD static void reflect(const EqP &, const double *UL, double *UR, double, double, double nx,
+                            double ny) {  // shallowwater/test/test.cu:63-77
+    double dot = UL[1] * nx + UL[2] * ny;
+    UR[0] = UL[0];
+    UR[1] = UL[1] - 2 * dot * nx;
+    UR[2] = UL[2] - 2 * dot * ny;
+  }
+  static constexpr bool outflow_uses_exact = false;
+};
+
+struct Maxwell {  // maxwells/maxwells.cu, U = (Hx, Hy, Ez)
+  static constexpr int N = 3;
+  DG_HD static bool physical(const EqP &, const double *) { return true; }
+  DG_HD static void flux(const EqP &q, const double *U, double *fx, double *fy) {
+    double imu = 1. / q.mu, ieps = 1. / q.eps;
+    fx[0] = 0.;
+    fx[1] = imu * U[2];
+    fx[2] = ieps * U[1];
+    fy[0] = -imu * U[2];
+    fy[1] = 0.;
+    fy[2] = -ieps * U[0];
+  }
+  DG_HD static void riemann(const EqP &q, const double *UL, const double *UR, double nx, double ny,
+                            double *F) {  // maxwells.cu:93-163, LLF with lambda = 1/sqrt(eps mu)
+    double imu = 1. / q.mu, ieps = 1. / q.eps, lam = fabs(1. / sqrt(q.eps * q.mu));
+    double ez = UL[2] + UR[2], hx = UL[0] + UR[0], hy = UL[1] + UR[1];
+    F[0] = 0.5 * (-imu * ez * ny + lam * (UL[0] - UR[0]));
+    F[1] = 0.5 * (imu * ez * nx + lam * (UL[1] - UR[1]));
+    F[2] = 0.5 * (ieps * (hy * nx - hx * ny) + lam * (UL[2] - UR[2]));
+  }
+  DG_HD static double mean_speed(const EqP &q, const double *) { return fabs(1. / sqrt(q.eps * q.mu)); }
+  DG_HD static void reflect(const EqP &, const double *UL, double *UR, double, double, double nx,
+                            double ny) {  // maxwells/cmirror/cmirror.cu:63-77
+    double dot = UL[0] * nx + UL[1] * ny;
+    UR[2] = UL[2];
+    UR[0] = UL[0] - 2 * dot * nx;
+    UR[1] = UL[1] - 2 * dot * ny;
+  }
+  static constexpr bool outflow_uses_exact = false;
+};
+
+// ghost state of a boundary side (eval_boundary, conserv_kernels.cu:820-843)
+template <class Eq>
+DG_HD void ghost_state(const EqP &q, int code, const double *UL, double *UR, double x, double y,
+                       double t, double nx, double ny) {
+  double G[4] = {0, 0, 0, 0};
+  if (code == -4) {  // transmissive (new)
+    for (int n = 0; n < Eq::N; n++) G[n] = UL[n];
+  } else if (code == -3) {  // inflow = the problem's exact state
+    exact_state(q, G, x, y, t);
+  } else if (code == -2) {  // outflow
+    if (Eq::outflow_uses_exact) exact_state(q, G, x, y, t);
+  } else {  // reflect
+    Eq::reflect(q, UL, G, x, y, nx, ny);
+  }
+  for (int n = 0; n < Eq::N; n++) UR[n] = G[n];
+}
+
+}  // namespace dg

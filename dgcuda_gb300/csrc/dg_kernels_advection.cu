@@ -1,0 +1,6 @@
+// dg_kernels_advection.cu -- kernel instances for the Advection module, p = 0..5.
+#include "dg_kernels.cuh"
+
+namespace dg {
+const Ops &ops_advection() { return Launch<Advection>::ops(); }
+}  // namespace dg

@@ -1,0 +1,6 @@
+// dg_kernels_euler.cu -- kernel instances for the Euler module, p = 0..5.
+#include "dg_kernels.cuh"
+
+namespace dg {
+const Ops &ops_euler() { return Launch<Euler>::ops(); }
+}  // namespace dg

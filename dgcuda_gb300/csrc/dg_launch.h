@@ -1,0 +1,99 @@
+// dg_launch.h -- host-side launch interface of the sm_103a kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+#include "dg_tables_data.h"
+
+namespace dg {
+
+struct EqP;
+
+// Device-resident mesh in internal (space-filling-curve) element order.
+// Per-element arrays are rows of length Kp (K rounded up to 32) so every
+// row of the [var][mode][elem] state starts 256-byte aligned.
+struct DevMesh {
+  int K = 0, Kp = 0, S = 0, Sb = 0;
+  double *geo = nullptr;  // 5 rows: xr, yr, xs, ys, 1/J
+  double *vtx = nullptr;  // 6 rows: V1x, V1y, V2x, V2y, V3x, V3y
+  double *jac = nullptr;  // 1 row: J
+  int *esd = nullptr;     // 3 rows: side index * 2 + (element is the side's right element)
+  int *nbr = nullptr;     // 3 rows: neighbour across face f (itself at a boundary)
+  int4 *side = nullptr;   // S: left, right (>= 0) or boundary code (< 0), left face, right face
+  double *sgeo = nullptr; // 3 rows of S: nx, ny, len / 2
+  double *bxy = nullptr;  // 4 rows of Sb: start and end vertex of the left face (boundary sides)
+  int *perm = nullptr;    // K: internal index -> caller's (.pmsh) index
+};
+
+// device scalars used by graph-captured steps
+struct DevScalars {
+  double t;         // current time
+  double dt;        // current step
+  double one;       // 1.0 (dt of a plain right-hand side)
+  double zero;      // 0.0
+  double dmin;      // minimum inscribed diameter
+  double cfl;       // CFL number
+  double fixed_dt;  // > 0: use it instead of the CFL step
+  double endtime;   // > 0: shorten the last step to land here
+  unsigned long long lam_bits;  // max wave speed (non-negative double as bits)
+  long long steps;  // steps taken with dt > 0
+  int status;       // 0 ok, 4 NaN or non-positive CFL step
+  int last;         // 1 when this step was shortened to land on endtime
+};
+
+struct Ctx {
+  cudaStream_t st = nullptr;
+  DevMesh m;
+  int p = 1, eq = 0, N = 1, np = 3;
+  const EqP *q = nullptr;         // host copy of the equation parameters
+  const void *tab = nullptr;      // host Tab<p> image
+  double *T = nullptr;            // traces [elem][face][j][var]
+  double *Fh = nullptr;           // face fluxes [side][j][var], scaled by len/2 * w_j
+  DevScalars *ds = nullptr;       // device scalars
+};
+
+struct Ops {
+  // edge traces of u; flattens (in u) any element with a non-physical trace
+  void (*trace)(const Ctx &, double *u);
+  // numerical flux on every side at time *t + tcoef * *dt
+  void (*face)(const Ctx &, const double *t, double tcoef);
+  // out = ca * un + cb * us + cc * dt * (du/dt of us); out may alias us or un
+  void (*element)(const Ctx &, double *us, const double *un, double *out, double ca, double cb,
+                  double cc, const double *dtp);
+  // Barth-Jespersen limiter in place
+  void (*limit)(const Ctx &, double *u);
+  // max cell-mean wave speed into ds->lam_bits (atomic max)
+  void (*lambda)(const Ctx &, const double *u);
+  // L2 projection of the problem's initial condition
+  void (*init)(const Ctx &, double *u);
+  // per-block partial sums of the squared L2 error, [nblocks][N]; returns nblocks
+  int (*l2err)(const Ctx &, const double *u, double t, double *partial);
+};
+
+const Ops &ops_advection();
+const Ops &ops_euler();
+const Ops &ops_shallow_water();
+const Ops &ops_maxwell();
+
+// per-order table image (Tab<p>) built from the generic tabulation
+size_t tab_bytes(int p);
+void build_tab(int p, const dg_order_tables &src, void *dst);
+
+// helpers (dg_kernels_common.cu)
+void launch_permute_in(cudaStream_t st, const double *user, double *internal, const int *perm,
+                       int rows, int K, int Kp);
+void launch_permute_out(cudaStream_t st, const double *internal, double *user, const int *perm,
+                        int rows, int K, int Kp);
+// y = a * x + b * y over n entries (RK4 / RK2 combinations), dt-scaled when dts != 0
+void launch_axpby(cudaStream_t st, int n, double a, const double *x, double b, double *y);
+// z = x + a * y
+void launch_xpay(cudaStream_t st, int n, const double *x, double a, const double *y, double *z);
+void launch_rk4_final(cudaStream_t st, int n, double *c, const double *k1, const double *k2,
+                      const double *k3, const double *k4);
+// dt from lam_bits (or fixed_dt), clamped to endtime; order p for the (2p+1)
+void launch_compute_dt(cudaStream_t st, DevScalars *ds, int p);
+void launch_reset_lambda(cudaStream_t st, DevScalars *ds);
+void launch_advance_t(cudaStream_t st, DevScalars *ds);
+
+}  // namespace dg

@@ -1,0 +1,759 @@
+// dg_solver.cpp -- the solver object behind the C ABI (include/dg.h).
+//
+// Replaces the reference's host driver (run_dgcuda, init_gpu, set_quadrature,
+// the preval_* set-up and the time integrators; src/2d/conservation/main.cu,
+// time_integrator.cu) with one object per problem that owns its device
+// buffers and CUDA stream: no globals, so many solvers coexist.  Geometry is
+// computed here in FP64 on the host (the reference computes it on the GPU
+// with float sqrtf, conserv_kernels.cu:412-585) and uploaded once.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "dg_device.cuh"
+#include "dg_internal.h"
+#include "dg_launch.h"
+
+using dg::fail;
+
+namespace {
+
+struct ProfEvent {
+  int kind;
+  cudaEvent_t a, b;
+};
+const char *kKindName[] = {"trace", "face", "element", "limit", "cfl", "rk"};
+constexpr int kKinds = 6;
+
+}  // namespace
+
+struct dg_solver {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  dg_equation eq = DG_EULER;
+  int p = 1, N = 4, np = 3, K = 0, S = 0;
+  dg_params prm{};
+  dg::EqP q{};
+  dg_order_tables tables{};
+  std::vector<char> tabimg;
+  dg::DevMesh m;
+  dg::Ctx ctx;
+  const dg::Ops *ops = nullptr;
+  double *U = nullptr, *W = nullptr, *k[4] = {nullptr, nullptr, nullptr, nullptr};
+  double *ubuf = nullptr, *partial = nullptr, *T = nullptr, *Fh = nullptr;
+  dg::DevScalars *ds = nullptr;
+  double dmin = 0;
+  size_t ndof_p = 0;  // N * np * Kp
+  // graphs per (scheme, limiter)
+  std::map<int, cudaGraphExec_t> graphs;
+  std::map<int, long long> graph_launches;
+  bool profiling = false;
+  std::vector<ProfEvent> pending;
+  std::vector<cudaEvent_t> pool;
+  long long prof_n[kKinds] = {0};
+  double prof_ms[kKinds] = {0};
+  long long launches = 0;
+  std::vector<void *> allocs;
+};
+
+namespace {
+
+dg_status cuda_fail(cudaError_t e, const char *what) {
+  return fail(DG_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                           \
+  do {                                                     \
+    cudaError_t e_ = (call);                               \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call);    \
+  } while (0)
+
+template <class T>
+dg_status dalloc(dg_solver *s, T **ptr, size_t count) {
+  void *p = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+  s->allocs.push_back(p);
+  *ptr = static_cast<T *>(p);
+  return DG_OK;
+}
+
+template <class T>
+dg_status upload(dg_solver *s, T **ptr, const std::vector<T> &h) {
+  dg_status st = dalloc(s, ptr, h.size());
+  if (st != DG_OK) return st;
+  if (!h.empty()) CK(cudaMemcpy(*ptr, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return DG_OK;
+}
+
+const dg::Ops *ops_for(dg_equation eq) {
+  switch (eq) {
+    case DG_ADVECTION: return &dg::ops_advection();
+    case DG_EULER: return &dg::ops_euler();
+    case DG_SHALLOW_WATER: return &dg::ops_shallow_water();
+    case DG_MAXWELL: return &dg::ops_maxwell();
+  }
+  return nullptr;
+}
+
+// ---- profiling: events around each launch when enabled ----
+cudaEvent_t take_event(dg_solver *s) {
+  if (!s->pool.empty()) {
+    cudaEvent_t e = s->pool.back();
+    s->pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  return e;
+}
+
+template <class F>
+void run(dg_solver *s, int kind, F &&f) {
+  if (s->profiling) {
+    ProfEvent pe{kind, take_event(s), take_event(s)};
+    cudaEventRecord(pe.a, s->st);
+    f();
+    cudaEventRecord(pe.b, s->st);
+    s->pending.push_back(pe);
+  } else {
+    f();
+  }
+  s->launches++;
+}
+
+void collect_profile(dg_solver *s) {
+  if (s->pending.empty()) return;
+  cudaStreamSynchronize(s->st);
+  for (auto &pe : s->pending) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, pe.a, pe.b);
+    s->prof_n[pe.kind]++;
+    s->prof_ms[pe.kind] += ms;
+    s->pool.push_back(pe.a);
+    s->pool.push_back(pe.b);
+  }
+  s->pending.clear();
+}
+
+enum { K_TRACE = 0, K_FACE = 1, K_ELEMENT = 2, K_LIMIT = 3, K_CFL = 4, K_RK = 5 };
+
+// one RK stage of the DG operator: out = ca*un + cb*us + cc*dt*L(us)
+void stage(dg_solver *s, double *us, const double *un, double *out, double ca, double cb,
+           double cc, double tcoef, const double *dtp) {
+  run(s, K_TRACE, [&] { s->ops->trace(s->ctx, us); });
+  run(s, K_FACE, [&] { s->ops->face(s->ctx, &s->ds->t, tcoef); });
+  run(s, K_ELEMENT, [&] { s->ops->element(s->ctx, us, un, out, ca, cb, cc, dtp); });
+}
+
+void limit(dg_solver *s, double *u) {
+  if (s->prm.limiter && s->np >= 3) run(s, K_LIMIT, [&] { s->ops->limit(s->ctx, u); });
+}
+
+void cfl(dg_solver *s) {
+  run(s, K_CFL, [&] { dg::launch_reset_lambda(s->st, s->ds); });
+  run(s, K_CFL, [&] { s->ops->lambda(s->ctx, s->U); });
+  run(s, K_CFL, [&] { dg::launch_compute_dt(s->st, s->ds, s->p); });
+}
+
+// one time step of `scheme` on s->U (launch sequence, capturable)
+void one_step(dg_solver *s, int scheme) {
+  const int n = (int)s->ndof_p;
+  const double *dt = &s->ds->dt;
+  cfl(s);
+  if (scheme == DG_SSP_RK3) {
+    // u1 = u + dt L(u); u2 = 3/4 u + 1/4 (u1 + dt L(u1)); u = 1/3 u + 2/3 (u2 + dt L(u2))
+    stage(s, s->U, nullptr, s->W, 0.0, 1.0, 1.0, 0.0, dt);
+    limit(s, s->W);
+    stage(s, s->W, s->U, s->W, 0.75, 0.25, 0.25, 1.0, dt);
+    limit(s, s->W);
+    stage(s, s->W, s->U, s->U, 1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0, 0.5, dt);
+    limit(s, s->U);
+    run(s, K_CFL, [&] { dg::launch_advance_t(s->st, s->ds); });
+  } else if (scheme == DG_RK4) {
+    // time_integrator.cu:198-400: t advanced first, limiter on each increment
+    run(s, K_CFL, [&] { dg::launch_advance_t(s->st, s->ds); });
+    double **k = s->k;
+    stage(s, s->U, nullptr, k[0], 0, 0, 1, 0.0, dt);
+    limit(s, k[0]);
+    run(s, K_RK, [&] { dg::launch_xpay(s->st, n, s->U, 0.5, k[0], k[1]); });
+    stage(s, k[1], nullptr, k[1], 0, 0, 1, 0.5, dt);
+    limit(s, k[1]);
+    run(s, K_RK, [&] { dg::launch_xpay(s->st, n, s->U, 0.5, k[1], k[2]); });
+    stage(s, k[2], nullptr, k[2], 0, 0, 1, 0.5, dt);
+    limit(s, k[2]);
+    run(s, K_RK, [&] { dg::launch_xpay(s->st, n, s->U, 1.0, k[2], k[3]); });
+    stage(s, k[3], nullptr, k[3], 0, 0, 1, 1.0, dt);
+    limit(s, k[3]);
+    run(s, K_RK, [&] { dg::launch_rk4_final(s->st, n, s->U, k[0], k[1], k[2], k[3]); });
+    limit(s, s->U);
+  } else {
+    // midpoint RK2, time_integrator.cu:557-690
+    run(s, K_CFL, [&] { dg::launch_advance_t(s->st, s->ds); });
+    double **k = s->k;
+    stage(s, s->U, nullptr, k[0], 0, 0, 1, 0.0, dt);
+    limit(s, k[0]);
+    run(s, K_RK, [&] { dg::launch_xpay(s->st, n, s->U, 0.5, k[0], k[0]); });
+    stage(s, k[0], nullptr, k[0], 0, 0, 1, 0.5, dt);
+    limit(s, k[0]);
+    run(s, K_RK, [&] { dg::launch_xpay(s->st, n, s->U, 1.0, k[0], s->U); });
+    limit(s, s->U);
+  }
+}
+
+dg_status ensure_rk_buffers(dg_solver *s) {
+  if (s->k[0]) return DG_OK;
+  for (int i = 0; i < 4; i++) {
+    dg_status st = dalloc(s, &s->k[i], s->ndof_p);
+    if (st != DG_OK) return st;
+    CK(cudaMemset(s->k[i], 0, s->ndof_p * sizeof(double)));
+  }
+  return DG_OK;
+}
+
+void drop_graphs(dg_solver *s) {
+  for (auto &g : s->graphs) cudaGraphExecDestroy(g.second);
+  s->graphs.clear();
+  s->graph_launches.clear();
+}
+
+dg_status get_graph(dg_solver *s, int scheme, cudaGraphExec_t *out) {
+  int key = scheme * 2 + (s->prm.limiter ? 1 : 0);
+  auto it = s->graphs.find(key);
+  if (it != s->graphs.end()) {
+    *out = it->second;
+    return DG_OK;
+  }
+  cudaGraph_t g;
+  long long before = s->launches;
+  CK(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
+  one_step(s, scheme);
+  cudaError_t e = cudaStreamEndCapture(s->st, &g);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+  s->launches = before;
+  s->graph_launches[key] = 0;
+  size_t nn = 0;
+  cudaGraphGetNodes(g, nullptr, &nn);
+  s->graph_launches[key] = (long long)nn;
+  cudaGraphExec_t ex;
+  e = cudaGraphInstantiate(&ex, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+  s->graphs[key] = ex;
+  *out = ex;
+  return DG_OK;
+}
+
+dg_status set_scalar(dg_solver *s, size_t offset, const void *v, size_t bytes) {
+  CK(cudaMemcpyAsync(reinterpret_cast<char *>(s->ds) + offset, v, bytes, cudaMemcpyHostToDevice,
+                     s->st));
+  CK(cudaStreamSynchronize(s->st));
+  return DG_OK;
+}
+
+dg_status read_scalars(dg_solver *s, dg::DevScalars *h) {
+  CK(cudaMemcpyAsync(h, s->ds, sizeof *h, cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  return DG_OK;
+}
+
+dg_status sync_check(dg_solver *s) {
+  cudaError_t e = cudaStreamSynchronize(s->st);
+  if (e != cudaSuccess) return cuda_fail(e, "kernel execution");
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+  return DG_OK;
+}
+
+// prepare device scalars for a run, then run nsteps (or until endtime)
+dg_status run_steps(dg_solver *s, int nsteps, int scheme, double fixed_dt, double endtime,
+                    double *t, int *taken) {
+  if (scheme < 0 || scheme > 2) return fail(DG_BAD_ARG, "unknown scheme");
+  if (scheme != DG_SSP_RK3) {
+    dg_status st = ensure_rk_buffers(s);
+    if (st != DG_OK) return st;
+  }
+  dg::DevScalars h{};
+  h.t = *t;
+  h.dt = 0;
+  h.one = 1.0;
+  h.zero = 0.0;
+  h.dmin = s->dmin;
+  h.cfl = s->prm.cfl;
+  h.fixed_dt = fixed_dt;
+  h.endtime = endtime;
+  dg_status st = set_scalar(s, 0, &h, sizeof h);
+  if (st != DG_OK) return st;
+  // the reference limits once before its step loop (time_integrator.cu:178-184)
+  limit(s, s->U);
+  cudaGraphExec_t g = nullptr;
+  if (!s->profiling) {
+    st = get_graph(s, scheme, &g);
+    if (st != DG_OK) return st;
+  }
+  int key = scheme * 2 + (s->prm.limiter ? 1 : 0);
+  auto launch_one = [&]() -> dg_status {
+    if (g) {
+      CK(cudaGraphLaunch(g, s->st));
+      s->launches += s->graph_launches[key];
+    } else {
+      one_step(s, scheme);
+    }
+    return DG_OK;
+  };
+  if (endtime > 0) {
+    const int batch = 8;
+    for (;;) {
+      for (int i = 0; i < batch; i++) {
+        st = launch_one();
+        if (st != DG_OK) return st;
+      }
+      collect_profile(s);
+      st = read_scalars(s, &h);
+      if (st != DG_OK) return st;
+      if (h.status) break;
+      if (h.t >= endtime) break;
+    }
+  } else {
+    for (int i = 0; i < nsteps; i++) {
+      st = launch_one();
+      if (st != DG_OK) return st;
+      if (s->profiling && (i % 16) == 15) collect_profile(s);
+    }
+    collect_profile(s);
+    st = read_scalars(s, &h);
+    if (st != DG_OK) return st;
+  }
+  st = sync_check(s);
+  if (st != DG_OK) return st;
+  *t = h.t;
+  if (taken) *taken = (int)h.steps;
+  if (h.status == 4) return fail(DG_NAN, "time step is NaN or not positive (non-finite state?)");
+  return DG_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" dg_status dg_solver_create(const dg_mesh *mesh, dg_equation eq, int p,
+                                      const dg_params *prm, int device, dg_solver **out) {
+  if (!mesh || !out) return fail(DG_BAD_ARG, "null argument");
+  *out = nullptr;
+  if (p < 0 || p > DG_PMAX) return fail(DG_BAD_ARG, "order p must be 0..5");
+  if (eq < DG_ADVECTION || eq > DG_MAXWELL) return fail(DG_BAD_ARG, "unknown equation");
+  dg_status vs = dg::validate_mesh(*mesh);
+  if (vs != DG_OK) return vs;
+  dg_params P;
+  if (prm) P = *prm;
+  else dg_params_default(&P);
+  if (P.problem < 0 || P.problem > DG_PB_MAXWELL_PLANE) return fail(DG_BAD_ARG, "unknown problem");
+  if (!(P.cfl > 0)) return fail(DG_BAD_ARG, "cfl must be positive");
+  if (eq == DG_EULER && !(P.gamma > 1)) return fail(DG_BAD_ARG, "gamma must be > 1");
+  if (eq == DG_SHALLOW_WATER && !(P.gravity > 0)) return fail(DG_BAD_ARG, "gravity must be > 0");
+  if (eq == DG_MAXWELL && !(P.mu > 0 && P.eps > 0)) return fail(DG_BAD_ARG, "mu, eps must be > 0");
+  int ndev = 0;
+  cudaError_t ce = cudaGetDeviceCount(&ndev);
+  if (ce != cudaSuccess || ndev == 0) return fail(DG_CUDA_ERROR, "no CUDA device available");
+  if (device < 0 || device >= ndev) return fail(DG_BAD_ARG, "device ordinal out of range");
+  CK(cudaSetDevice(device));
+
+  dg_solver *s = new dg_solver();
+  s->device = device;
+  s->eq = eq;
+  s->p = p;
+  s->prm = P;
+  static const int NV[4] = {1, 4, 3, 3};
+  s->N = NV[eq];
+  s->np = dg::np_of(p);
+  s->K = mesh->K;
+  s->S = mesh->S;
+  s->ops = ops_for(eq);
+  s->q.gamma = P.gamma;
+  s->q.g = P.gravity;
+  s->q.ax = P.ax;
+  s->q.ay = P.ay;
+  s->q.mu = P.mu;
+  s->q.eps = P.eps;
+  s->q.problem = P.problem;
+  for (int i = 0; i < 8; i++) s->q.prm[i] = P.prm[i];
+  s->tables = DG_TABLES[p];
+  s->tabimg.resize(dg::tab_bytes(p));
+  dg::build_tab(p, s->tables, s->tabimg.data());
+
+  auto bail = [&](dg_status st) {
+    dg_solver_destroy(s);
+    return st;
+  };
+  if (cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(fail(DG_CUDA_ERROR, "cudaStreamCreate failed"));
+
+  // ---- internal element order: Morton curve of the centroids ----
+  const int K = mesh->K, S = mesh->S;
+  const int Kp = (K + 31) / 32 * 32;
+  std::vector<int> perm = dg::sfc_order(*mesh);  // new -> old
+  std::vector<int> inv(K);
+  for (int e = 0; e < K; e++) inv[perm[e]] = e;
+  // ---- internal side order: boundary sides first (by code), then interior by first element ----
+  std::vector<int> sorder(S);
+  std::iota(sorder.begin(), sorder.end(), 0);
+  auto skey = [&](int sd) -> long long {
+    int r = mesh->right[sd];
+    if (r < 0) return (long long)(-r) * 0 - 10 + (-r);  // -9..-6: boundary, by code
+    int a = inv[mesh->left[sd]], b = inv[r];
+    return (long long)std::min(a, b) * 4 + 3;
+  };
+  std::stable_sort(sorder.begin(), sorder.end(), [&](int a, int b) { return skey(a) < skey(b); });
+  std::vector<int> snew(S);
+  for (int i = 0; i < S; i++) snew[sorder[i]] = i;
+  int Sb = 0;
+  while (Sb < S && mesh->right[sorder[Sb]] < 0) Sb++;
+
+  // ---- element arrays ----
+  std::vector<double> geo((size_t)5 * Kp, 0.0), vtx((size_t)6 * Kp, 0.0), jac(Kp, 1.0);
+  std::vector<int> esd((size_t)3 * Kp, 0), nbr((size_t)3 * Kp, 0);
+  double dmin = 1e300;
+  for (int e = 0; e < K; e++) {
+    int o = perm[e];
+    double x1 = mesh->V[0][o], y1 = mesh->V[1][o], x2 = mesh->V[2][o], y2 = mesh->V[3][o],
+           x3 = mesh->V[4][o], y3 = mesh->V[5][o];
+    double J = (x2 - x1) * (y3 - y1) - (x3 - x1) * (y2 - y1);  // preval_jacobian
+    geo[e] = x2 - x1;                                           // preval_partials
+    geo[(size_t)Kp + e] = y2 - y1;
+    geo[2 * (size_t)Kp + e] = x3 - x1;
+    geo[3 * (size_t)Kp + e] = y3 - y1;
+    geo[4 * (size_t)Kp + e] = 1.0 / J;
+    jac[e] = J;
+    const double v6[6] = {x1, y1, x2, y2, x3, y3};
+    for (int k = 0; k < 6; k++) vtx[(size_t)k * Kp + e] = v6[k];
+    // inscribed-circle diameter (preval_inscribed_circles, conserv_kernels.cu:428-445)
+    double a = std::sqrt((x1 - x2) * (x1 - x2) + (y1 - y2) * (y1 - y2));
+    double b = std::sqrt((x2 - x3) * (x2 - x3) + (y2 - y3) * (y2 - y3));
+    double c = std::sqrt((x1 - x3) * (x1 - x3) + (y1 - y3) * (y1 - y3));
+    double kk = 0.5 * (a + b + c);
+    double d = 2 * std::sqrt(kk * (kk - a) * (kk - b) * (kk - c)) / kk;
+    dmin = std::min(dmin, d);
+    for (int f = 0; f < 3; f++) {
+      int so = mesh->es[f][o];
+      bool right = !(mesh->left[so] == o && mesh->lsn[so] == f);
+      esd[(size_t)f * Kp + e] = snew[so] * 2 + (right ? 1 : 0);
+      int other = right ? mesh->left[so] : mesh->right[so];
+      nbr[(size_t)f * Kp + e] = other >= 0 ? inv[other] : e;
+    }
+  }
+  s->dmin = dmin;
+  // ---- side arrays ----
+  std::vector<int4> side(S);
+  std::vector<double> sgeo((size_t)3 * S), bxy((size_t)4 * std::max(Sb, 1));
+  for (int i = 0; i < S; i++) {
+    int so = sorder[i];
+    int L = mesh->left[so], R = mesh->right[so], lf = mesh->lsn[so];
+    side[i] = make_int4(inv[L], R >= 0 ? inv[R] : R, lf, R >= 0 ? mesh->rsn[so] : 0);
+    // normal from the side's vertices, pointed away from the left element's
+    // third vertex (preval_normals + preval_normals_direction, :481-569)
+    double dx = mesh->sx2[so] - mesh->sx1[so], dy = mesh->sy2[so] - mesh->sy1[so];
+    double len = std::sqrt(dx * dx + dy * dy);
+    double nx = -dy / len, ny = dx / len;
+    int va = lf, vb = (lf + 1) % 3, vc = (lf + 2) % 3;
+    double ax = mesh->V[2 * va][L], ay = mesh->V[2 * va + 1][L];
+    double bx = mesh->V[2 * vb][L], by = mesh->V[2 * vb + 1][L];
+    double cx = mesh->V[2 * vc][L], cy = mesh->V[2 * vc + 1][L];
+    double mx = (ax + bx) / 2., my = (ay + by) / 2.;
+    if (nx * (cx - mx) + ny * (cy - my) > 0) {
+      nx = -nx;
+      ny = -ny;
+    }
+    sgeo[i] = nx;
+    sgeo[(size_t)S + i] = ny;
+    sgeo[2 * (size_t)S + i] = len / 2;
+    if (i < Sb) {
+      bxy[i] = ax;
+      bxy[(size_t)Sb + i] = ay;
+      bxy[2 * (size_t)Sb + i] = bx;
+      bxy[3 * (size_t)Sb + i] = by;
+    }
+  }
+
+  // ---- device buffers ----
+  dg::DevMesh &m = s->m;
+  m.K = K;
+  m.Kp = Kp;
+  m.S = S;
+  m.Sb = Sb;
+  dg_status st;
+  if ((st = upload(s, &m.geo, geo)) != DG_OK) return bail(st);
+  if ((st = upload(s, &m.vtx, vtx)) != DG_OK) return bail(st);
+  if ((st = upload(s, &m.jac, jac)) != DG_OK) return bail(st);
+  if ((st = upload(s, &m.esd, esd)) != DG_OK) return bail(st);
+  if ((st = upload(s, &m.nbr, nbr)) != DG_OK) return bail(st);
+  if ((st = upload(s, &m.side, side)) != DG_OK) return bail(st);
+  if ((st = upload(s, &m.sgeo, sgeo)) != DG_OK) return bail(st);
+  if ((st = upload(s, &m.bxy, bxy)) != DG_OK) return bail(st);
+  if ((st = upload(s, &m.perm, perm)) != DG_OK) return bail(st);
+  s->ndof_p = (size_t)s->N * s->np * Kp;
+  size_t nuser = (size_t)s->N * s->np * K;
+  const int n1 = p + 1;
+  if ((st = dalloc(s, &s->U, s->ndof_p)) != DG_OK) return bail(st);
+  if ((st = dalloc(s, &s->W, s->ndof_p)) != DG_OK) return bail(st);
+  if ((st = dalloc(s, &s->ubuf, nuser)) != DG_OK) return bail(st);
+  if ((st = dalloc(s, &s->T, (size_t)K * 3 * n1 * s->N)) != DG_OK) return bail(st);
+  if ((st = dalloc(s, &s->Fh, (size_t)S * n1 * s->N)) != DG_OK) return bail(st);
+  if ((st = dalloc(s, &s->partial, (size_t)s->N * ((K + 127) / 128 + 1))) != DG_OK) return bail(st);
+  if ((st = dalloc(s, &s->ds, 1)) != DG_OK) return bail(st);
+  if (cudaMemset(s->U, 0, s->ndof_p * sizeof(double)) != cudaSuccess ||
+      cudaMemset(s->W, 0, s->ndof_p * sizeof(double)) != cudaSuccess ||
+      cudaMemset(s->ds, 0, sizeof(dg::DevScalars)) != cudaSuccess)
+    return bail(fail(DG_CUDA_ERROR, "cudaMemset failed"));
+  dg::DevScalars h{};
+  h.one = 1.0;
+  h.dmin = dmin;
+  h.cfl = P.cfl;
+  if (cudaMemcpy(s->ds, &h, sizeof h, cudaMemcpyHostToDevice) != cudaSuccess)
+    return bail(fail(DG_CUDA_ERROR, "cudaMemcpy failed"));
+
+  dg::Ctx &c = s->ctx;
+  c.st = s->st;
+  c.m = m;
+  c.p = p;
+  c.eq = eq;
+  c.N = s->N;
+  c.np = s->np;
+  c.q = &s->q;
+  c.tab = s->tabimg.data();
+  c.T = s->T;
+  c.Fh = s->Fh;
+  c.ds = s->ds;
+  *out = s;
+  return DG_OK;
+}
+
+extern "C" void dg_solver_destroy(dg_solver *s) {
+  if (!s) return;
+  cudaSetDevice(s->device);
+  if (s->st) cudaStreamSynchronize(s->st);
+  drop_graphs(s);
+  for (auto &pe : s->pending) {
+    cudaEventDestroy(pe.a);
+    cudaEventDestroy(pe.b);
+  }
+  for (auto e : s->pool) cudaEventDestroy(e);
+  for (void *p : s->allocs) cudaFree(p);
+  if (s->st) cudaStreamDestroy(s->st);
+  delete s;
+}
+
+extern "C" dg_status dg_solver_sizes(const dg_solver *s, int *N, int *n_p, int *K, int *S) {
+  if (!s) return fail(DG_BAD_ARG, "null solver");
+  if (N) *N = s->N;
+  if (n_p) *n_p = s->np;
+  if (K) *K = s->K;
+  if (S) *S = s->S;
+  return DG_OK;
+}
+
+extern "C" void *dg_solver_stream(dg_solver *s) { return s ? (void *)s->st : nullptr; }
+
+extern "C" dg_status dg_solver_set_tables(dg_solver *s, int n_q, int n_1, const double *basis,
+                                          const double *grad_x, const double *grad_y,
+                                          const double *side, const double *vertex,
+                                          const double *w, const double *r1, const double *r2,
+                                          const double *r_oned, const double *w_oned) {
+  if (!s || !basis || !grad_x || !grad_y || !side || !vertex || !w || !r1 || !r2 || !r_oned ||
+      !w_oned)
+    return fail(DG_BAD_ARG, "null argument");
+  if (n_q != dg::nq_of(s->p) || n_1 != s->p + 1)
+    return fail(DG_BAD_ARG, "table sizes do not match the order p");
+  dg_order_tables t{};
+  int np = s->np;
+  t.n_p = np;
+  t.n_q = n_q;
+  t.n_1 = n_1;
+  for (int q = 0; q < n_q; q++) {
+    t.r[q] = r1[q];
+    t.s[q] = r2[q];
+    t.w[q] = w[q];
+    for (int i = 0; i < np; i++) {
+      t.B[q][i] = basis[i * n_q + q];
+      t.GR[q][i] = grad_x[i * n_q + q];
+      t.GS[q][i] = grad_y[i * n_q + q];
+    }
+  }
+  for (int j = 0; j < n_1; j++) {
+    t.t1[j] = r_oned[j];
+    t.w1[j] = w_oned[j];
+    for (int f = 0; f < 3; f++)
+      for (int i = 0; i < np; i++) t.E[f][j][i] = side[f * np * n_1 + i * n_1 + j];
+  }
+  for (int v = 0; v < 3; v++)
+    for (int i = 0; i < np; i++) t.V[v][i] = vertex[i * 3 + v];
+  s->tables = t;
+  dg::build_tab(s->p, s->tables, s->tabimg.data());
+  drop_graphs(s);
+  return DG_OK;
+}
+
+extern "C" dg_status dg_init(dg_solver *s) {
+  if (!s) return fail(DG_BAD_ARG, "null solver");
+  CK(cudaSetDevice(s->device));
+  run(s, K_RK, [&] { s->ops->init(s->ctx, s->U); });
+  collect_profile(s);
+  return sync_check(s);
+}
+
+extern "C" dg_status dg_set_state(dg_solver *s, const double *C) {
+  if (!s || !C) return fail(DG_BAD_ARG, "null argument");
+  CK(cudaSetDevice(s->device));
+  size_t n = (size_t)s->N * s->np * s->K;
+  CK(cudaMemcpyAsync(s->ubuf, C, n * sizeof(double), cudaMemcpyHostToDevice, s->st));
+  dg::launch_permute_in(s->st, s->ubuf, s->U, s->m.perm, s->N * s->np, s->K, s->m.Kp);
+  return sync_check(s);
+}
+
+extern "C" dg_status dg_get_state(dg_solver *s, double *C) {
+  if (!s || !C) return fail(DG_BAD_ARG, "null argument");
+  CK(cudaSetDevice(s->device));
+  size_t n = (size_t)s->N * s->np * s->K;
+  dg::launch_permute_out(s->st, s->U, s->ubuf, s->m.perm, s->N * s->np, s->K, s->m.Kp);
+  CK(cudaMemcpyAsync(C, s->ubuf, n * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+  return sync_check(s);
+}
+
+extern "C" dg_status dg_set_state_device(dg_solver *s, const double *C) {
+  if (!s || !C) return fail(DG_BAD_ARG, "null argument");
+  CK(cudaSetDevice(s->device));
+  dg::launch_permute_in(s->st, C, s->U, s->m.perm, s->N * s->np, s->K, s->m.Kp);
+  return sync_check(s);
+}
+
+extern "C" dg_status dg_get_state_device(dg_solver *s, double *C) {
+  if (!s || !C) return fail(DG_BAD_ARG, "null argument");
+  CK(cudaSetDevice(s->device));
+  dg::launch_permute_out(s->st, s->U, C, s->m.perm, s->N * s->np, s->K, s->m.Kp);
+  return sync_check(s);
+}
+
+extern "C" dg_status dg_rhs(dg_solver *s, double t, const double *C, double *dCdt) {
+  if (!s || !C || !dCdt) return fail(DG_BAD_ARG, "null argument");
+  CK(cudaSetDevice(s->device));
+  size_t n = (size_t)s->N * s->np * s->K;
+  double *in = s->W, *out = nullptr;
+  dg_status st = ensure_rk_buffers(s);
+  if (st != DG_OK) return st;
+  out = s->k[0];
+  st = set_scalar(s, offsetof(dg::DevScalars, t), &t, sizeof t);
+  if (st != DG_OK) return st;
+  CK(cudaMemcpyAsync(s->ubuf, C, n * sizeof(double), cudaMemcpyHostToDevice, s->st));
+  dg::launch_permute_in(s->st, s->ubuf, in, s->m.perm, s->N * s->np, s->K, s->m.Kp);
+  stage(s, in, nullptr, out, 0.0, 0.0, 1.0, 0.0, &s->ds->one);
+  dg::launch_permute_out(s->st, out, s->ubuf, s->m.perm, s->N * s->np, s->K, s->m.Kp);
+  CK(cudaMemcpyAsync(dCdt, s->ubuf, n * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+  collect_profile(s);
+  return sync_check(s);
+}
+
+extern "C" dg_status dg_limit(dg_solver *s) {
+  if (!s) return fail(DG_BAD_ARG, "null solver");
+  CK(cudaSetDevice(s->device));
+  if (s->np >= 3) run(s, K_LIMIT, [&] { s->ops->limit(s->ctx, s->U); });
+  collect_profile(s);
+  return sync_check(s);
+}
+
+extern "C" dg_status dg_step(dg_solver *s, int nsteps, dg_scheme scheme, double fixed_dt,
+                             double *t) {
+  if (!s || !t) return fail(DG_BAD_ARG, "null argument");
+  if (nsteps < 0) return fail(DG_BAD_ARG, "nsteps must be >= 0");
+  CK(cudaSetDevice(s->device));
+  return run_steps(s, nsteps, scheme, fixed_dt, 0.0, t, nullptr);
+}
+
+extern "C" dg_status dg_advance_to(dg_solver *s, double T, dg_scheme scheme, double *t,
+                                   int *nsteps) {
+  if (!s || !t) return fail(DG_BAD_ARG, "null argument");
+  if (!(T > *t)) {
+    if (nsteps) *nsteps = 0;
+    return DG_OK;
+  }
+  CK(cudaSetDevice(s->device));
+  return run_steps(s, 0, scheme, 0.0, T, t, nsteps);
+}
+
+extern "C" dg_status dg_cfl(dg_solver *s, double *dt, double *lambda_max, double *d_min) {
+  if (!s) return fail(DG_BAD_ARG, "null solver");
+  CK(cudaSetDevice(s->device));
+  dg::DevScalars h{};
+  dg_status st = read_scalars(s, &h);
+  if (st != DG_OK) return st;
+  h.fixed_dt = 0;
+  h.endtime = 0;
+  h.cfl = s->prm.cfl;
+  h.dmin = s->dmin;
+  h.status = 0;
+  st = set_scalar(s, 0, &h, sizeof h);
+  if (st != DG_OK) return st;
+  cfl(s);
+  collect_profile(s);
+  st = read_scalars(s, &h);
+  if (st != DG_OK) return st;
+  if (dt) *dt = h.dt;
+  if (lambda_max) *lambda_max = __builtin_bit_cast(double, h.lam_bits);
+  if (d_min) *d_min = s->dmin;
+  if (h.status == 4) return fail(DG_NAN, "wave speed is NaN");
+  return DG_OK;
+}
+
+extern "C" dg_status dg_l2_error(dg_solver *s, double t, double *err) {
+  if (!s || !err) return fail(DG_BAD_ARG, "null argument");
+  CK(cudaSetDevice(s->device));
+  int nb = s->ops->l2err(s->ctx, s->U, t, s->partial);
+  s->launches++;
+  std::vector<double> h((size_t)nb * s->N);
+  CK(cudaMemcpyAsync(h.data(), s->partial, h.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                     s->st));
+  dg_status st = sync_check(s);
+  if (st != DG_OK) return st;
+  for (int n = 0; n < s->N; n++) {
+    double a = 0;
+    for (int b = 0; b < nb; b++) a += h[(size_t)b * s->N + n];
+    err[n] = std::sqrt(a);
+  }
+  return DG_OK;
+}
+
+extern "C" dg_status dg_profile_enable(dg_solver *s, int on) {
+  if (!s) return fail(DG_BAD_ARG, "null solver");
+  collect_profile(s);
+  s->profiling = on != 0;
+  return DG_OK;
+}
+
+extern "C" dg_status dg_profile_get(dg_solver *s, const char *kernel, long long *launches,
+                                    double *ms) {
+  if (!s || !kernel) return fail(DG_BAD_ARG, "null argument");
+  collect_profile(s);
+  for (int k = 0; k < kKinds; k++)
+    if (!std::strcmp(kernel, kKindName[k])) {
+      if (launches) *launches = s->prof_n[k];
+      if (ms) *ms = s->prof_ms[k];
+      return DG_OK;
+    }
+  return fail(DG_BAD_ARG, std::string("unknown kernel name ") + kernel);
+}
+
+extern "C" dg_status dg_profile_reset(dg_solver *s) {
+  if (!s) return fail(DG_BAD_ARG, "null solver");
+  collect_profile(s);
+  for (int k = 0; k < kKinds; k++) {
+    s->prof_n[k] = 0;
+    s->prof_ms[k] = 0;
+  }
+  return DG_OK;
+}
+
+extern "C" long long dg_kernel_launches(const dg_solver *s) { return s ? s->launches : 0; }

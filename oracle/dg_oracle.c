@@ -35,7 +35,8 @@
  * (euler.cu:92-116).  The oracle uses the order-free rule the GPU solver
  * implements: an element whose edge traces contain a non-physical value is
  * flattened to its mean before any face uses it; an element with a
- * non-physical volume value uses its mean for the whole volume integral.
+ * non-physical volume value is flattened too and its mean is used for the
+ * whole volume integral (and by the RK update that follows).
  */
 #include <math.h>
 #include <stdlib.h>
@@ -602,9 +603,11 @@ static void dg_operator(or_solver *o, double *C, double t, double dt, double *ou
         for (int n = 0; n < N; n++) U[n] += C[CI(n, i, e)] * o->B[q][i];
       if (!physical(o, U)) flat = 1;
     }
-    if (flat) {
+    if (flat) { /* the element's state becomes its mean (C_global write, euler.cu:98-108) */
 #pragma omp atomic
       o->flattened++;
+      for (int n = 0; n < N; n++)
+        for (int i = 1; i < np; i++) C[CI(n, i, e)] = 0.;
     }
     memset(acc, 0, sizeof acc);
     for (int q = 0; q < nq; q++) {
