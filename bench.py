@@ -1,0 +1,356 @@
+#!/usr/bin/env python3
+"""Throughput benchmark of the GB300 RK-DG solver.
+
+Workload (one "step" = one SSP-RK3 time step = 3 RK stages of the DG
+right-hand side, its stage update and the slope limiter over the whole mesh):
+plain 2D Euler (gamma 1.4), four-quadrant Riemann data, 1024 x 1024 squares
+cut into 2,097,152 triangles jittered by +-0.1h (seed 3), transmissive
+boundaries, p = 3 (10 modes, 83.9 M degrees of freedom), Rusanov flux,
+Barth-Jespersen limiter, FP64.  Synthetic inputs; the state (671 MB) is
+larger than the 129 MB L2, so no flush is needed between steps.
+
+Metric: DOF-stage updates per second (K * N * n_p * 3 per step), whole job.
+`value` is device time (CUDA events on the solver's stream) with the state
+resident in HBM; `e2e` runs the same steps through the C ABI with the state
+copied in from pinned host memory and out again every step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+With N > 1 (torchrun, one rank per GPU) every rank runs an independent
+replica (the solver does not shard) and `value` is the sum of
+the ranks' DOF-stage updates over the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DOF-stage updates/s at p=1..4 vs HBM roofline; batched/plain and adjoint/fwd ratio"
+UNIT = "DOF-stage/s"
+GAMMA = 1.4
+
+
+def workload_config(n, p, steps_note):
+    K = 2 * n * n
+    return {
+        "workload": "Euler four-quadrant Riemann, %dx%d squares -> %d triangles (jitter 0.1h, "
+                    "seed 3), p=%d, Rusanov, SSP-RK3, Barth-Jespersen limiter, transmissive"
+                    % (n, n, K, p),
+        "equation": "euler", "p": p, "elements": K, "vars": 4, "modes": (p + 1) * (p + 2) // 2,
+        "stages_per_step": 3, "cfl": 0.2, "precision": "fp64",
+        "l2": "no flush: state %.0f MB > 129 MB L2" % (K * 4 * (p + 1) * (p + 2) / 2 * 8 / 1e6),
+        "parallelism": steps_note,
+    }
+
+
+def alg_bytes_per_elem(N, npm):
+    # 3 state streams (stage input, u^n, stage output) + 56 B of geometry
+    return 8 * N * npm * 3 + 56
+
+
+def alg_flops_per_elem(N, npm, nq, n1):
+    # FMA = 2 flops: solution at area points, metric fold, gradient
+    # projection, traces at 3 n1 edge points, surface projection, epilogue
+    vol = nq * N * npm * 2 + nq * N * 8 + nq * N * (npm - 1) * 4
+    surf = 3 * n1 * N * npm * 2 * 2
+    return vol + surf + N * npm * 6
+
+
+def clocks_sampler(idx, stop, out):
+    q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    try:
+        p = subprocess.Popen(["nvidia-smi", "-i", str(idx), "--query-gpu=" + q,
+                              "--format=csv,noheader,nounits", "-lms", "200"],
+                             stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+    except OSError:
+        return
+    def reader():
+        for line in p.stdout:
+            out.append(line.strip())
+    th = threading.Thread(target=reader, daemon=True)
+    th.start()
+    stop.wait()
+    p.terminate()
+    try:
+        p.wait(timeout=5)
+    except subprocess.TimeoutExpired:
+        p.kill()
+    th.join(timeout=2)
+
+
+def summarize_clocks(lines):
+    sm, mx, reasons = [], 0.0, set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for l in lines:
+        f = [x.strip() for x in l.split(",")]
+        if len(f) < 9:
+            continue
+        try:
+            sm.append(float(f[1]))
+            mx = max(mx, float(f[2]))
+        except ValueError:
+            continue
+        for k, name in enumerate(names):
+            if f[5 + k].lower().startswith("active"):
+                reasons.add(name)
+    if not sm:
+        return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+    return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+            "samples": len(sm)}
+
+
+def cpu_baseline(n_sample, p, steps, threads=None):
+    """The oracle (C restatement of the reference method, OpenMP) on a
+    bounded sample of the workload: n_sample^2 squares, `steps` SSP-RK3
+    steps, all host threads."""
+    import dgcuda_gb300 as dg
+    from oracle import oracle as orc
+    if threads:
+        orc.set_threads(threads)
+    mesh = dg.Mesh.square(n_sample, n_sample, jitter=0.1, seed=3, bc=(-4, -4, -4, -4))
+    o = orc.Oracle.from_mesh(mesh, dg.EULER, p, orc.prm_vec(gamma=GAMMA),
+                             dg.PROBLEMS["euler_riemann4"])
+    c = o.init()
+    c, _, _ = o.step(c, 1, 0, 1, 0.2)  # warm-up
+    t0 = time.perf_counter()
+    c, _, n = o.step(c, steps, 0, 1, 0.2)
+    dt = time.perf_counter() - t0
+    npm = (p + 1) * (p + 2) // 2
+    cores = orc.lib().or_max_threads()
+    return {"value": mesh.K * 4 * npm * 3 * n / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "seconds": dt,
+            "sample": "%d SSP-RK3 steps (limiter on) of the same problem on %dx%d squares "
+                      "(%d triangles), p=%d, C oracle with OpenMP" % (n, n_sample, n_sample,
+                                                                      mesh.K, p)}
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return 0
+    n_sample = 512
+    cb = None
+    # each timed step is one SSP-RK3 step of the sampled mesh; the run is
+    # capped at ~90 s of CPU time
+    import dgcuda_gb300 as dg
+    from oracle import oracle as orc
+    mesh = dg.Mesh.square(n_sample, n_sample, jitter=0.1, seed=3, bc=(-4, -4, -4, -4))
+    o = orc.Oracle.from_mesh(mesh, dg.EULER, args.p, orc.prm_vec(gamma=GAMMA),
+                             dg.PROBLEMS["euler_riemann4"])
+    c = o.init()
+    for _ in range(args.warmup):
+        c, _, _ = o.step(c, 1, 0, 1, 0.2)
+    done, t0 = 0, time.perf_counter()
+    while done < args.steps:
+        c, _, _ = o.step(c, 1, 0, 1, 0.2)
+        done += 1
+        if time.perf_counter() - t0 > 90:
+            break
+    dt = time.perf_counter() - t0
+    npm = (args.p + 1) * (args.p + 2) // 2
+    value = mesh.K * 4 * npm * 3 * done / dt
+    cores = orc.lib().or_max_threads()
+    cb = {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+          "sample": "%d SSP-RK3 steps (limiter on) of the same problem on %dx%d squares (%d "
+                    "triangles), p=%d; the reference's CUDA cannot run on this CPU, so its "
+                    "method restated in C (oracle/dg_oracle.c, pinned bit-exact to the "
+                    "reference's kernels) runs with OpenMP" % (done, n_sample, n_sample, mesh.K,
+                                                               args.p)}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": done,
+            "warmup": args.warmup, "ms_per_step": dt / done * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(args.n, args.p, "cpu, %d threads" % cores),
+            "impl": "reference", "cpu_baseline": cb,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--p", type=int, default=3)
+    ap.add_argument("--n", type=int, default=1024, help="squares per side")
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--no-sweep", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        return run_reference(args, rank)
+
+    import torch
+    import torch.distributed as dist
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    import dgcuda_gb300 as dg
+    dg.load_library()
+    n, p = args.n, args.p
+    N, npm = 4, (p + 1) * (p + 2) // 2
+    nq, n1 = [1, 3, 6, 12, 16, 25][p], p + 1
+    mesh = dg.Mesh.square(n, n, jitter=0.1, seed=3, bc=(-4, -4, -4, -4))
+    K = mesh.K
+    s = dg.Solver(mesh, dg.EULER, p, device=local, problem="euler_riemann4", limiter=1, cfl=0.2,
+                  gamma=GAMMA)
+    s.init_conditions()
+    t = s.step(args.warmup, dg.SSP_RK3, 0.0)
+    stream = torch.cuda.ExternalStream(s.stream(), device=local)
+    fp64_peak = dg.measure_fp64_peak(local)
+
+    # ---- timed region: K steps, per-kernel CUDA events on the solver stream ----
+    s.profile(True)
+    s.profile_reset()
+    launches0 = s.kernel_launches()
+    clk_lines, stop = [], threading.Event()
+    th = threading.Thread(target=clocks_sampler, args=(local, stop, clk_lines), daemon=True)
+    th.start()
+    time.sleep(0.5)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    t = s.step(args.steps, dg.SSP_RK3, t)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        dist.barrier()
+    stop.set()
+    th.join(timeout=10)
+    launches = s.kernel_launches() - launches0
+    kern = {k: s.profile_get(k) for k in ("trace", "face", "element", "limit", "cfl", "rk")}
+    s.profile(False)
+    if world > 1:
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    dof_stage = K * N * npm * 3 * args.steps
+    value = dof_stage * world / (ms / 1e3)
+
+    # ---- roofline of the dominant kernel ----
+    stage_ms = {k: v[1] / max(v[0], 1) for k, v in kern.items()}
+    dom = max(("trace", "face", "element", "limit"), key=lambda k: kern[k][1])
+    elem_ms = stage_ms[dom]
+    bpe = alg_bytes_per_elem(N, npm)
+    achieved = K * bpe / (elem_ms / 1e3) / 1e9
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    traffic = None
+    try:
+        tr = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
+        key = "euler_p%d_%s" % (p, dom)
+        if key in tr:
+            traffic = tr[key]["dram_bytes_per_element"] * K
+    except (OSError, ValueError, KeyError):
+        pass
+    stage_total_ms = sum(kern[k][1] for k in ("trace", "face", "element", "limit")) / (
+        3 * args.steps)
+    fpe = alg_flops_per_elem(N, npm, nq, n1)
+    fp64_achieved = K * fpe / (stage_total_ms / 1e3) / 1e12
+
+    # ---- e2e through the C ABI with pinned host buffers ----
+    e2e = None
+    if args.e2e_steps > 0:
+        host = torch.empty((N, npm, K), dtype=torch.float64, pin_memory=True)
+        h = host.numpy()
+        s.get_state(out=h)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        te = t
+        for _ in range(args.e2e_steps):
+            s.set_state(h)
+            te = s.step(1, dg.SSP_RK3, te)
+            s.get_state(out=h)
+        el = time.perf_counter() - t0
+        if world > 1:
+            tt = torch.tensor([el], device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            el = float(tt.item())
+        nb = N * npm * K * 8
+        e2e = {"value": K * N * npm * 3 * args.e2e_steps * world / el, "unit": UNIT,
+               "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb,
+               "steps": args.e2e_steps,
+               "note": "per step: dg_set_state from pinned host memory, dg_step(1), "
+                       "dg_get_state to host; host wall clock"}
+
+    # ---- order sweep p = 1..4 (shorter runs, same mesh) ----
+    sweep = {}
+    if not args.no_sweep:
+        for ps in (1, 2, 3, 4):
+            if ps == p:
+                sweep[str(ps)] = value / world
+                continue
+            ss = dg.Solver(mesh, dg.EULER, ps, device=local, problem="euler_riemann4", limiter=1,
+                           cfl=0.2, gamma=GAMMA)
+            ss.init_conditions()
+            tt0 = ss.step(2, dg.SSP_RK3, 0.0)
+            st2 = torch.cuda.ExternalStream(ss.stream(), device=local)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            nst = 10
+            a.record(st2)
+            ss.step(nst, dg.SSP_RK3, tt0)
+            b.record(st2)
+            torch.cuda.synchronize()
+            nps = (ps + 1) * (ps + 2) // 2
+            sweep[str(ps)] = K * 4 * nps * 3 * nst / (a.elapsed_time(b) / 1e3)
+            ss.close()
+
+    cb = None
+    if rank == 0 and not args.no_cpu:
+        cb = cpu_baseline(512, p, 3)
+
+    if rank == 0:
+        clocks = summarize_clocks(clk_lines)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(n, p, "replicas x%d (no sharding)" % world),
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
+                         "alg_bytes_per_element": bpe,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+                         "binding": "fp64",
+                         "fp64": {"achieved_tflops": fp64_achieved, "peak_tflops": fp64_peak,
+                                  "frac": fp64_achieved / fp64_peak,
+                                  "alg_flops_per_element_stage": fpe,
+                                  "peak_source": "dg_measure_fp64_peak (FP64 FMA loop, live)"}},
+            "kernels_ms_per_launch": stage_ms,
+            "kernels_launches": {k: v[0] for k, v in kern.items()},
+            "p_sweep": sweep,
+            "cpu_baseline": cb, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
+            "final_time": t,
+        }
+        print(json.dumps(line), flush=True)
+    s.close()
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -100,6 +100,7 @@ def _declare(L):
         "dg_profile_get": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_longlong), _dp]),
         "dg_profile_reset": (C.c_int, [C.c_void_p]),
         "dg_kernel_launches": (C.c_longlong, [C.c_void_p]),
+        "dg_measure_fp64_peak": (C.c_int, [C.c_int, _dp]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(L, name, None)
@@ -107,6 +108,14 @@ def _declare(L):
             continue
         fn.restype = res
         fn.argtypes = args
+
+
+def measure_fp64_peak(device=0):
+    """FP64 FMA throughput of the GPU in TFLOP/s."""
+    L = load_library()
+    v = C.c_double()
+    _check(L.dg_measure_fp64_peak(device, C.byref(v)))
+    return v.value
 
 
 def _check(st):
@@ -226,10 +235,16 @@ class Solver:
         c = np.ascontiguousarray(c, dtype=np.float64).reshape(self.shape)
         _check(self._L.dg_set_state(self._h, _dptr(c)))
 
-    def get_state(self):
-        c = np.empty(self.shape)
-        _check(self._L.dg_get_state(self._h, _dptr(c)))
-        return c
+    def get_state(self, out=None):
+        """State in the reference layout [var][mode][elem]; fills `out` (a
+        C-contiguous float64 array, e.g. over pinned memory) when given."""
+        if out is None:
+            out = np.empty(self.shape)
+        elif (out.dtype != np.float64 or not out.flags["C_CONTIGUOUS"]
+              or out.size != self.N * self.n_p * self.K):
+            raise ValueError("out must be a C-contiguous float64 array of the state's size")
+        _check(self._L.dg_get_state(self._h, _dptr(out)))
+        return out
 
     def eval_rhs(self, c, t=0.0):
         c = np.ascontiguousarray(c, dtype=np.float64).reshape(self.shape)

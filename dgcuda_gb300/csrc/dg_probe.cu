@@ -1,0 +1,54 @@
+// dg_probe.cu -- FP64 FMA throughput of the current GPU (the binding roof of
+// the DG kernels on GB300), measured with CUDA events.
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "dg_internal.h"
+
+namespace {
+__global__ void k_fma64(double *out, int iters, double a, double b) {
+  double x[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) x[k] = threadIdx.x * 1e-3 + k;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int k = 0; k < 8; k++) x[k] = fma(x[k], a, b);
+  }
+  double s = 0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) s += x[k];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+}  // namespace
+
+extern "C" dg_status dg_measure_fp64_peak(int device, double *tflops) {
+  if (!tflops) return dg::fail(DG_BAD_ARG, "null argument");
+  if (cudaSetDevice(device) != cudaSuccess) return dg::fail(DG_CUDA_ERROR, "cudaSetDevice");
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  const int blocks = sms * 8, threads = 256, iters = 2000;
+  double *d = nullptr;
+  if (cudaMalloc(&d, sizeof(double) * blocks * threads) != cudaSuccess)
+    return dg::fail(DG_CUDA_ERROR, "cudaMalloc");
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  for (int rep = 0; rep < 3; rep++) {
+    cudaEventRecord(e0);
+    k_fma64<<<blocks, threads>>>(d, iters, 0.999999, 1e-7);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) best = ms;
+  }
+  cudaError_t err = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d);
+  if (err != cudaSuccess) return dg::fail(DG_CUDA_ERROR, cudaGetErrorString(err));
+  *tflops = 2.0 * 8 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
+  return DG_OK;
+}

@@ -171,6 +171,10 @@ dg_status dg_profile_reset(dg_solver *s);
 /* launches of the solver's kernels since creation (all kinds) */
 long long dg_kernel_launches(const dg_solver *s);
 
+/* FP64 FMA throughput of `device` in TFLOP/s (the binding roof of the DG
+ * kernels on GB300), timed with CUDA events; no reference counterpart */
+dg_status dg_measure_fp64_peak(int device, double *tflops);
+
 #ifdef __cplusplus
 }
 #endif
