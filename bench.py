@@ -109,6 +109,20 @@ def summarize_clocks(lines):
             "samples": len(sm)}
 
 
+def reduce_replicas(units, seconds, dist=None):
+    """Whole-job throughput of independent replicas: the units all ranks
+    processed over the slowest rank's time (max over ranks)."""
+    if dist is None or not dist.is_available() or not dist.is_initialized():
+        return units / seconds, seconds
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([seconds], dtype=torch.float64, device=dev)
+    u = torch.tensor([units], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(u.item()) / float(t.item()), float(t.item())
+
+
 def cpu_baseline(n_sample, p, steps, threads=None):
     """The oracle (C restatement of the reference method, OpenMP) on a
     bounded sample of the workload: n_sample^2 squares, `steps` SSP-RK3
@@ -240,12 +254,9 @@ def main():
     launches = s.kernel_launches() - launches0
     kern = {k: s.profile_get(k) for k in ("trace", "face", "element", "limit", "cfl", "rk")}
     s.profile(False)
-    if world > 1:
-        tt = torch.tensor([ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
     dof_stage = K * N * npm * 3 * args.steps
-    value = dof_stage * world / (ms / 1e3)
+    value, sec = reduce_replicas(dof_stage, ms / 1e3, dist if world > 1 else None)
+    ms = sec * 1e3
 
     # ---- roofline of the dominant kernel ----
     stage_ms = {k: v[1] / max(v[0], 1) for k, v in kern.items()}
@@ -286,12 +297,10 @@ def main():
             te = s.step(1, dg.SSP_RK3, te)
             s.get_state(out=h)
         el = time.perf_counter() - t0
-        if world > 1:
-            tt = torch.tensor([el], device="cuda")
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            el = float(tt.item())
+        e2e_value, el = reduce_replicas(K * N * npm * 3 * args.e2e_steps, el,
+                                        dist if world > 1 else None)
         nb = N * npm * K * 8
-        e2e = {"value": K * N * npm * 3 * args.e2e_steps * world / el, "unit": UNIT,
+        e2e = {"value": e2e_value, "unit": UNIT,
                "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb,
                "steps": args.e2e_steps,
                "note": "per step: dg_set_state from pinned host memory, dg_step(1), "

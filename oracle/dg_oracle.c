@@ -164,6 +164,25 @@ int or_set_tables(or_solver *o, int nq, int n1, const double *basis, const doubl
   return 0;
 }
 
+/* the tabulation in the reference's flat layout (basis, grad_x, grad_y,
+ * side, vertex, w, r1, r2, r_oned, w_oned; see or_set_tables) */
+int or_get_tables(const or_solver *o, double *out) {
+  int np = o->np, nq = o->nq, n1 = o->n1;
+  double *p = out;
+  for (int i = 0; i < np; i++) for (int q = 0; q < nq; q++) *p++ = o->B[q][i];
+  for (int i = 0; i < np; i++) for (int q = 0; q < nq; q++) *p++ = o->GR[q][i];
+  for (int i = 0; i < np; i++) for (int q = 0; q < nq; q++) *p++ = o->GS[q][i];
+  for (int f = 0; f < 3; f++)
+    for (int i = 0; i < np; i++) for (int j = 0; j < n1; j++) *p++ = o->E[f][j][i];
+  for (int i = 0; i < np; i++) for (int v = 0; v < 3; v++) *p++ = o->VT[v][i];
+  for (int q = 0; q < nq; q++) *p++ = o->w[q];
+  for (int q = 0; q < nq; q++) *p++ = o->r[q];
+  for (int q = 0; q < nq; q++) *p++ = o->s[q];
+  for (int j = 0; j < n1; j++) *p++ = o->t1[j];
+  for (int j = 0; j < n1; j++) *p++ = o->w1[j];
+  return (int)(p - out);
+}
+
 /* ---------------- problems (initial / boundary / exact states) ---------------- */
 static void exact_state(const or_solver *o, double *U, double x, double y, double t) {
   const double *P = o->prm;

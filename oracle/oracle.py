@@ -59,6 +59,7 @@ def lib():
         L.or_min_diameter.argtypes = [C.c_void_p]
         L.or_flattened.argtypes = [C.c_void_p]
         L.or_set_threads.argtypes = [C.c_int]
+        L.or_get_tables.argtypes = [C.c_void_p, _dp]
         _L = L
     return _L
 
@@ -112,6 +113,13 @@ class Oracle:
         rc = self.L.or_set_tables(self.h, nq, n1, *[_d(a) for a in parts])
         if rc:
             raise ValueError("table size mismatch")
+
+    def tables(self):
+        """The oracle's tabulation in the reference's flat layout."""
+        npm, nq, n1 = self.np, self.nq_for(), self.p + 1
+        out = np.empty(3 * npm * nq + 3 * npm * n1 + 3 * npm + 3 * nq + 2 * n1)
+        n = self.L.or_get_tables(self.h, _d(out))
+        return out[:n]
 
     def nq_for(self):
         return [1, 3, 6, 12, 16, 25][self.p]
