@@ -96,4 +96,18 @@ void launch_compute_dt(cudaStream_t st, DevScalars *ds, int p);
 void launch_reset_lambda(cudaStream_t st, DevScalars *ds);
 void launch_advance_t(cudaStream_t st, DevScalars *ds);
 
+// what other files need to launch a solver's kernels
+struct SolverView {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  const Ops *ops = nullptr;
+  Ctx ctx;
+  int N = 0, np = 0, p = 0, K = 0, S = 0;
+};
+
+}  // namespace dg
+
+struct dg_solver;
+namespace dg {
+SolverView solver_view(dg_solver *s);
 }  // namespace dg

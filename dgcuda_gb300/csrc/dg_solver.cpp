@@ -757,3 +757,20 @@ extern "C" dg_status dg_profile_reset(dg_solver *s) {
 }
 
 extern "C" long long dg_kernel_launches(const dg_solver *s) { return s ? s->launches : 0; }
+
+namespace dg {
+// read-only view of a solver for entry points defined in other files
+SolverView solver_view(dg_solver *s) {
+  SolverView v;
+  v.device = s->device;
+  v.st = s->st;
+  v.ops = s->ops;
+  v.ctx = s->ctx;
+  v.N = s->N;
+  v.np = s->np;
+  v.p = s->p;
+  v.K = s->K;
+  v.S = s->S;
+  return v;
+}
+}  // namespace dg

@@ -171,6 +171,18 @@ dg_status dg_profile_reset(dg_solver *s);
 /* launches of the solver's kernels since creation (all kinds) */
 long long dg_kernel_launches(const dg_solver *s);
 
+/* du/dt like dg_rhs, for callers that may not allocate device memory while
+ * evaluating it (an application that owns all device memory and forbids
+ * allocation after set-up, a latency-critical loop, a stream capture).
+ * C_device and dCdt_device are the caller's device buffers in the reference
+ * layout; all working memory comes from a static 32 MiB array that every GPU
+ * loading the library holds until exit.  Larger problems get DG_UNSUPPORTED.
+ * The first call on a device looks up that array's address (make it before
+ * any stream capture).  Calls that overlap on the GPU race on the array.
+ * No counterpart in the reference. */
+dg_status dg_rhs_device_noalloc(dg_solver *s, double t, const double *C_device,
+                                double *dCdt_device);
+
 /* FP64 FMA throughput of `device` in TFLOP/s (the binding roof of the DG
  * kernels on GB300), timed with CUDA events; no reference counterpart */
 dg_status dg_measure_fp64_peak(int device, double *tflops);
