@@ -101,6 +101,7 @@ def _declare(L):
         "dg_profile_reset": (C.c_int, [C.c_void_p]),
         "dg_kernel_launches": (C.c_longlong, [C.c_void_p]),
         "dg_measure_fp64_peak": (C.c_int, [C.c_int, _dp]),
+        "dg_eval_vertices": (C.c_int, [C.c_void_p, C.c_int, _dp]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(L, name, None)
@@ -283,6 +284,13 @@ class Solver:
         err = np.empty(self.N)
         _check(self._L.dg_l2_error(self._h, t, _dptr(err)))
         return err
+
+    def eval_u(self, var):
+        """Values of variable `var` at the vertices V1, V2, V3 of every element,
+        shape (3, K) (eval_u, conserv_kernels.cu:1284)."""
+        out = np.empty((3, self.K))
+        _check(self._L.dg_eval_vertices(self._h, var, _dptr(out)))
+        return out
 
     def stream(self):
         return self._L.dg_solver_stream(self._h)

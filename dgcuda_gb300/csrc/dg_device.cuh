@@ -30,6 +30,7 @@ struct Tab {
   double E[3][N1][NP];   // phi_i at edge point j of face f (face 2 reversed)
   double r[NQ], s[NQ], w[NQ];
   double t1[N1], w1[N1];
+  double V[3][NP];       // phi_i at the vertices (0,0), (1,0), (0,1)
 };
 
 // equation / problem parameters (kernel parameter)

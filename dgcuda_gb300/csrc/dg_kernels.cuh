@@ -22,6 +22,11 @@
 //              out = ca*u^n + cb*u_s + cc*dt*du/dt.
 //   k_limit    Barth-Jespersen limiter in place (limit_c, :640-720).
 //
+// SSP-RK3 steps skip k_trace after the first stage: k_element<TR=true>
+// writes the traces of its output as it stores it, and k_limit_tr limits
+// from those traces and rebuilds the ones it changes, so T always holds what
+// k_trace would have computed from the next stage's input.
+//
 // FP64 is the binding resource on GB300 (the FP64 pipe runs at 1/62 of the
 // FP32 rate), so the design minimises FP64 instructions: every basis value
 // is a constant-bank operand (tables are __grid_constant__ parameters and
@@ -171,12 +176,15 @@ __device__ __forceinline__ bool volume(const Tab<P> &tab, const EqP &q,
   return ok;
 }
 
-template <class Eq, int P>
+// TR: also write the edge traces of `out` into T (what k_trace would compute
+// from it at the start of the next stage, bit for bit) and, when `check` is
+// set, flatten an element whose new traces are non-physical
+template <class Eq, int P, bool TR>
 __global__ void __launch_bounds__(kBlock) k_element(
     const __grid_constant__ Tab<P> tab, const __grid_constant__ EqP q, double *us,
     const double *un, double *out, const double *__restrict__ Fh, const int *__restrict__ esd,
     const double *__restrict__ geo, const double *dtp, double ca, double cb, double cc, int K,
-    int Kp) {
+    int Kp, double *__restrict__ T, int check) {
   constexpr int N = Eq::N, NP = Tab<P>::NP, N1 = Tab<P>::N1;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= K) return;
@@ -234,7 +242,39 @@ __global__ void __launch_bounds__(kBlock) k_element(
       double v = fma(s, acc[n][i], cb * c[n][i]);
       if (ca != 0.0) v = fma(ca, un[o], v);
       out[o] = v;
+      if (TR) acc[n][i] = v;
     }
+  if (TR) {
+    double *Te = T + (size_t)e * (3 * N1 * N);
+    bool bad = false;
+#pragma unroll
+    for (int f = 0; f < 3; f++)
+#pragma unroll
+      for (int j = 0; j < N1; j++) {
+        double U[N];
+#pragma unroll
+        for (int n = 0; n < N; n++) {
+          double a = acc[n][0] * tab.E[f][j][0];
+#pragma unroll
+          for (int i = 1; i < NP; i++) a = fma(acc[n][i], tab.E[f][j][i], a);
+          U[n] = a;
+        }
+        bad |= !Eq::physical(q, U);
+#pragma unroll
+        for (int n = 0; n < N; n++) Te[(f * N1 + j) * N + n] = U[n];
+      }
+    if (check && bad) {
+#pragma unroll
+      for (int n = 0; n < N; n++) {
+#pragma unroll
+        for (int i = 1; i < NP; i++) out[(size_t)(n * NP + i) * Kp + e] = 0.0;
+#pragma unroll
+        for (int f = 0; f < 3; f++)
+#pragma unroll
+          for (int j = 0; j < N1; j++) Te[(f * N1 + j) * N + n] = acc[n][0] * tab.E[f][j][0];
+      }
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -283,6 +323,82 @@ __global__ void __launch_bounds__(kBlock) k_limit(const __grid_constant__ Tab<P>
       w[(size_t)2 * Kp + e] = c[2] * alpha;
 #pragma unroll
       for (int i = 3; i < NP; i++) w[(size_t)i * Kp + e] = 0.0;  // p > 1: drop higher modes
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// The same limiter reading the edge traces k_element<TR> left in T instead of
+// re-evaluating them; a limited variable's traces are rebuilt from its
+// limited modes, then the positivity rule of k_trace is applied to the final
+// traces.  T ends up holding exactly what k_trace would compute from the
+// limited state.
+template <class Eq, int P>
+__global__ void __launch_bounds__(kBlock) k_limit_tr(const __grid_constant__ Tab<P> tab,
+                                                     const __grid_constant__ EqP q, double *u,
+                                                     double *__restrict__ T,
+                                                     const int *__restrict__ nbr, int K,
+                                                     int Kp) {
+  constexpr int N = Eq::N, NP = Tab<P>::NP, N1 = Tab<P>::N1;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= K) return;
+  const int nb0 = nbr[e], nb1 = nbr[(size_t)Kp + e], nb2 = nbr[2 * (size_t)Kp + e];
+  const double phi0 = tab.B[0][0];
+  double *Te = T + (size_t)e * (3 * N1 * N);
+  double c0[N];
+  bool bad = false;
+#pragma unroll
+  for (int n = 0; n < N; n++) {
+    double *row = u + (size_t)(n * NP) * Kp;
+    c0[n] = row[e];
+    const double Uc = c0[n] * phi0;
+    const double m0 = row[nb0] * phi0, m1 = row[nb1] * phi0, m2 = row[nb2] * phi0;
+    const double Umin = fmin(Uc, fmin(m0, fmin(m1, m2)));
+    const double Umax = fmax(Uc, fmax(m0, fmax(m1, m2)));
+    double up = 0.0, dn = 0.0;
+#pragma unroll
+    for (int k = 0; k < 3 * N1; k++) {
+      const double d = Te[k * N + n] - Uc;
+      up = fmax(up, d);
+      dn = fmax(dn, -d);
+    }
+    double alpha = 1.0;
+    if (up > 0.0) alpha = fmin(alpha, (Uc - Umin) / up);
+    if (dn > 0.0) alpha = fmin(alpha, (Umax - Uc) / dn);
+    if (alpha < 0.0) alpha = 0.0;
+    if (alpha < 1.0) {
+      const double c1 = row[(size_t)1 * Kp + e] * alpha, c2 = row[(size_t)2 * Kp + e] * alpha;
+      row[(size_t)1 * Kp + e] = c1;
+      row[(size_t)2 * Kp + e] = c2;
+#pragma unroll
+      for (int i = 3; i < NP; i++) row[(size_t)i * Kp + e] = 0.0;
+#pragma unroll
+      for (int f = 0; f < 3; f++)
+#pragma unroll
+        for (int j = 0; j < N1; j++) {
+          double a = c0[n] * tab.E[f][j][0];
+          a = fma(c1, tab.E[f][j][1], a);
+          a = fma(c2, tab.E[f][j][2], a);
+          Te[(f * N1 + j) * N + n] = a;
+        }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 3 * N1; k++) {
+    double U[N];
+#pragma unroll
+    for (int n = 0; n < N; n++) U[n] = Te[k * N + n];
+    bad |= !Eq::physical(q, U);
+  }
+  if (bad) {
+#pragma unroll
+    for (int n = 0; n < N; n++) {
+#pragma unroll
+      for (int i = 1; i < NP; i++) u[(size_t)(n * NP + i) * Kp + e] = 0.0;
+#pragma unroll
+      for (int f = 0; f < 3; f++)
+#pragma unroll
+        for (int j = 0; j < N1; j++) Te[(f * N1 + j) * N + n] = c0[n] * tab.E[f][j][0];
     }
   }
 }
@@ -401,6 +517,27 @@ __global__ void __launch_bounds__(kBlock) k_l2err(const __grid_constant__ Tab<P>
 }
 
 // ---------------------------------------------------------------------------
+// values of variable `var` at the three vertices (eval_u, conserv_kernels.cu:1284-1307)
+template <class Eq, int P>
+__global__ void __launch_bounds__(kBlock) k_vertex(const __grid_constant__ Tab<P> tab,
+                                                   const double *__restrict__ u, int var,
+                                                   double *__restrict__ out, int K, int Kp) {
+  constexpr int NP = Tab<P>::NP;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= K) return;
+  double c[NP];
+#pragma unroll
+  for (int i = 0; i < NP; i++) c[i] = u[(size_t)(var * NP + i) * Kp + e];
+#pragma unroll
+  for (int v = 0; v < 3; v++) {
+    double a = 0.0;
+#pragma unroll
+    for (int i = 0; i < NP; i++) a += c[i] * tab.V[v][i];
+    out[(size_t)v * Kp + e] = a;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // launchers: dispatch on p to the template instance
 // ---------------------------------------------------------------------------
 inline unsigned nblk(int n) { return (unsigned)((n + kBlock - 1) / kBlock); }
@@ -436,9 +573,22 @@ struct Launch {
   static void element(const Ctx &c, double *us, const double *un, double *out, double ca,
                       double cb, double cc, const double *dtp) {
     if (!c.m.K) return;
-    DG_DISPATCH_P((k_element<Eq, P><<<nblk(c.m.K), kBlock, 0, c.st>>>(
+    DG_DISPATCH_P((k_element<Eq, P, false><<<nblk(c.m.K), kBlock, 0, c.st>>>(
         tab<P>(c), *c.q, us, un, out, c.Fh, c.m.esd, c.m.geo, dtp, ca, cb, cc, c.m.K,
-        c.m.Kp)));
+        c.m.Kp, nullptr, 0)));
+  }
+  static void element_tr(const Ctx &c, double *us, const double *un, double *out, double ca,
+                         double cb, double cc, const double *dtp, int check) {
+    if (!c.m.K) return;
+    DG_DISPATCH_P((k_element<Eq, P, true><<<nblk(c.m.K), kBlock, 0, c.st>>>(
+        tab<P>(c), *c.q, us, un, out, c.Fh, c.m.esd, c.m.geo, dtp, ca, cb, cc, c.m.K,
+        c.m.Kp, c.T, check)));
+  }
+  static void limit_tr(const Ctx &c, double *u) {
+    if (!c.m.K || c.p < 1) return;
+    DG_DISPATCH_P((k_limit_tr<Eq, P><<<nblk(c.m.K), kBlock, 0, c.st>>>(tab<P>(c), *c.q, u, c.T,
+                                                                        c.m.nbr, c.m.K,
+                                                                        c.m.Kp)));
   }
   static void limit(const Ctx &c, double *u) {
     if (!c.m.K || c.p < 1) return;
@@ -458,10 +608,16 @@ struct Launch {
         tab<P>(c), *c.q, u, c.m.vtx, c.m.jac, t, partial, c.m.K, c.m.Kp)));
     return (int)nblk(c.m.K);
   }
+
+  static void vertex(const Ctx &c, const double *u, int var, double *out) {
+    DG_DISPATCH_P((k_vertex<Eq, P><<<nblk(c.m.K), kBlock, 0, c.st>>>(tab<P>(c), u, var, out,
+                                                                      c.m.K, c.m.Kp)));
+  }
 #undef DG_DISPATCH_P
 
   static const Ops &ops() {
-    static const Ops o = {trace, face, element, limit, lambda, init, l2err};
+    static const Ops o = {trace, face, element, limit, lambda, init, l2err, element_tr,
+                          limit_tr, vertex};
     return o;
   }
 };

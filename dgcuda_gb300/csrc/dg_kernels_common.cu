@@ -27,6 +27,8 @@ static void fill_tab(const dg_order_tables &s, Tab<P> *t) {
     t->t1[j] = s.t1[j];
     t->w1[j] = s.w1[j];
   }
+  for (int v = 0; v < 3; v++)
+    for (int i = 0; i < NP; i++) t->V[v][i] = s.V[v][i];
 }
 
 size_t tab_bytes(int p) {

@@ -69,6 +69,14 @@ struct Ops {
   void (*init)(const Ctx &, double *u);
   // per-block partial sums of the squared L2 error, [nblocks][N]; returns nblocks
   int (*l2err)(const Ctx &, const double *u, double t, double *partial);
+  // element() that also leaves the traces of `out` in T (the next stage's
+  // k_trace, fused); check = apply the positivity rule to them here
+  void (*element_tr)(const Ctx &, double *us, const double *un, double *out, double ca,
+                     double cb, double cc, const double *dtp, int check);
+  // limit() reading and updating the traces in T (after element_tr)
+  void (*limit_tr)(const Ctx &, double *u);
+  // values of variable var at the three vertices, rows of Kp: out[v][elem]
+  void (*vertex)(const Ctx &, const double *u, int var, double *out);
 };
 
 const Ops &ops_advection();

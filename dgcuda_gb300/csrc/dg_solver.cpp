@@ -44,7 +44,7 @@ struct dg_solver {
   dg::Ctx ctx;
   const dg::Ops *ops = nullptr;
   double *U = nullptr, *W = nullptr, *k[4] = {nullptr, nullptr, nullptr, nullptr};
-  double *ubuf = nullptr, *partial = nullptr, *T = nullptr, *Fh = nullptr;
+  double *ubuf = nullptr, *partial = nullptr, *T = nullptr, *Fh = nullptr, *vbuf = nullptr;
   dg::DevScalars *ds = nullptr;
   double dmin = 0;
   size_t ndof_p = 0;  // N * np * Kp
@@ -155,6 +155,17 @@ void limit(dg_solver *s, double *u) {
   if (s->prm.limiter && s->np >= 3) run(s, K_LIMIT, [&] { s->ops->limit(s->ctx, u); });
 }
 
+// a stage whose input traces are already in T (left by the previous stage);
+// it leaves the traces of `out` -- limited when the limiter is on -- in T
+void fused_stage(dg_solver *s, double *us, const double *un, double *out, double ca, double cb,
+                 double cc, double tcoef, const double *dtp) {
+  const bool lim = s->prm.limiter && s->np >= 3;
+  run(s, K_FACE, [&] { s->ops->face(s->ctx, &s->ds->t, tcoef); });
+  run(s, K_ELEMENT,
+      [&] { s->ops->element_tr(s->ctx, us, un, out, ca, cb, cc, dtp, lim ? 0 : 1); });
+  if (lim) run(s, K_LIMIT, [&] { s->ops->limit_tr(s->ctx, out); });
+}
+
 void cfl(dg_solver *s) {
   run(s, K_CFL, [&] { dg::launch_reset_lambda(s->st, s->ds); });
   run(s, K_CFL, [&] { s->ops->lambda(s->ctx, s->U); });
@@ -167,13 +178,11 @@ void one_step(dg_solver *s, int scheme) {
   const double *dt = &s->ds->dt;
   cfl(s);
   if (scheme == DG_SSP_RK3) {
-    // u1 = u + dt L(u); u2 = 3/4 u + 1/4 (u1 + dt L(u1)); u = 1/3 u + 2/3 (u2 + dt L(u2))
-    stage(s, s->U, nullptr, s->W, 0.0, 1.0, 1.0, 0.0, dt);
-    limit(s, s->W);
-    stage(s, s->W, s->U, s->W, 0.75, 0.25, 0.25, 1.0, dt);
-    limit(s, s->W);
-    stage(s, s->W, s->U, s->U, 1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0, 0.5, dt);
-    limit(s, s->U);
+    // u1 = u + dt L(u); u2 = 3/4 u + 1/4 (u1 + dt L(u1)); u = 1/3 u + 2/3 (u2 + dt L(u2));
+    // T holds the traces of u on entry (run_steps) and of the new u on exit
+    fused_stage(s, s->U, nullptr, s->W, 0.0, 1.0, 1.0, 0.0, dt);
+    fused_stage(s, s->W, s->U, s->W, 0.75, 0.25, 0.25, 1.0, dt);
+    fused_stage(s, s->W, s->U, s->U, 1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0, 0.5, dt);
     run(s, K_CFL, [&] { dg::launch_advance_t(s->st, s->ds); });
   } else if (scheme == DG_RK4) {
     // time_integrator.cu:198-400: t advanced first, limiter on each increment
@@ -291,6 +300,8 @@ dg_status run_steps(dg_solver *s, int nsteps, int scheme, double fixed_dt, doubl
   if (st != DG_OK) return st;
   // the reference limits once before its step loop (time_integrator.cu:178-184)
   limit(s, s->U);
+  // SSP-RK3 stages find their input traces in T (fused_stage)
+  if (scheme == DG_SSP_RK3) run(s, K_TRACE, [&] { s->ops->trace(s->ctx, s->U); });
   cudaGraphExec_t g = nullptr;
   if (!s->profiling) {
     st = get_graph(s, scheme, &g);
@@ -506,6 +517,7 @@ extern "C" dg_status dg_solver_create(const dg_mesh *mesh, dg_equation eq, int p
   if ((st = dalloc(s, &s->Fh, (size_t)S * n1 * s->N)) != DG_OK) return bail(st);
   if ((st = dalloc(s, &s->partial, (size_t)s->N * ((K + 127) / 128 + 1))) != DG_OK) return bail(st);
   if ((st = dalloc(s, &s->ds, 1)) != DG_OK) return bail(st);
+  if ((st = dalloc(s, &s->vbuf, (size_t)6 * Kp)) != DG_OK) return bail(st);
   if (cudaMemset(s->U, 0, s->ndof_p * sizeof(double)) != cudaSuccess ||
       cudaMemset(s->W, 0, s->ndof_p * sizeof(double)) != cudaSuccess ||
       cudaMemset(s->ds, 0, sizeof(dg::DevScalars)) != cudaSuccess)
@@ -724,6 +736,19 @@ extern "C" dg_status dg_l2_error(dg_solver *s, double t, double *err) {
     err[n] = std::sqrt(a);
   }
   return DG_OK;
+}
+
+extern "C" dg_status dg_eval_vertices(dg_solver *s, int var, double *uv) {
+  if (!s || !uv) return fail(DG_BAD_ARG, "null argument");
+  if (var < 0 || var >= s->N) return fail(DG_BAD_ARG, "variable index out of range");
+  CK(cudaSetDevice(s->device));
+  run(s, K_RK, [&] { s->ops->vertex(s->ctx, s->U, var, s->vbuf); });
+  double *user = s->vbuf + (size_t)3 * s->m.Kp;
+  dg::launch_permute_out(s->st, s->vbuf, user, s->m.perm, 3, s->K, s->m.Kp);
+  CK(cudaMemcpyAsync(uv, user, (size_t)3 * s->K * sizeof(double), cudaMemcpyDeviceToHost,
+                     s->st));
+  collect_profile(s);
+  return sync_check(s);
 }
 
 extern "C" dg_status dg_profile_enable(dg_solver *s, int on) {

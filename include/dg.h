@@ -160,6 +160,12 @@ dg_status dg_cfl(dg_solver *s, double *dt, double *lambda_max, double *d_min);
  * conserv_kernels.cu:1432-1479, main.cu:859-875) */
 dg_status dg_l2_error(dg_solver *s, double t, double *err);
 
+/* values of variable `var` of the current state at the three vertices of
+ * every element: uv[0*K + e], uv[1*K + e], uv[2*K + e] at V1, V2, V3 of
+ * element e (.pmsh order) -- eval_u + the copies of write_U
+ * (conserv_kernels.cu:1284-1307, main.cu:69-116) */
+dg_status dg_eval_vertices(dg_solver *s, int var, double *uv);
+
 /* Timing of the solver's own kernels (CUDA events around each launch on the
  * solver stream).  When enabled, dg_step launches kernels directly instead
  * of replaying a CUDA graph. */

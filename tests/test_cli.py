@@ -1,0 +1,50 @@
+"""The dgcuda command line (run_dgcuda's flags, main.cu:481-599)."""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+CLI = os.path.join(ROOT, "dgcuda_gb300", "dgcuda")
+
+
+def test_usage_and_bad_options(dglib):
+    r = subprocess.run([CLI, "-h"], capture_output=True, text=True)
+    assert r.returncode == 1 and "Usage: dgcuda" in r.stdout
+    r = subprocess.run([CLI, "--bogus", "x", "m.pmsh"], capture_output=True, text=True)
+    assert r.returncode == 1
+    r = subprocess.run([CLI, "-n", "9", "m.pmsh"], capture_output=True, text=True)
+    assert r.returncode == 1
+
+
+def test_missing_mesh_is_an_error_not_a_crash(dglib, tmp_path):
+    r = subprocess.run([CLI, "-n", "1", "-t", "1", str(tmp_path / "none.pmsh")],
+                       capture_output=True, text=True)
+    assert r.returncode == 1 and "mesh file not found" in r.stderr
+
+
+@pytest.mark.gpu
+def test_cli_matches_library(dglib, tmp_path):
+    dg = dglib
+    vtx = (5.0, 5.0, 5.0, 1.0, 1.0, 10.0)
+    mesh = dg.Mesh.square(16, 16, box=(0, 10, 0, 10), jitter=0.15, seed=3)
+    path = str(tmp_path / "v.pmsh")
+    mesh.write(path)
+    out = str(tmp_path / "out")
+    r = subprocess.run([CLI, "-n", "2", "-T", "0.1", "-e", "--eq", "euler", "--problem",
+                        "euler_vortex", "--prm", ",".join(map(str, vtx)), "--scheme", "ssprk3",
+                        "--cfl", "0.2", "-o", out, path], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    errs = [float(x) for x in re.findall(r"L2 U\d error\s+= (\S+)", r.stdout)]
+    s = dg.Solver(mesh, dg.EULER, 2, problem="euler_vortex", prm=vtx, cfl=0.2)
+    s.init_conditions()
+    t, _ = s.advance_to(0.1, dg.SSP_RK3)
+    np.testing.assert_allclose(errs, s.eval_error_L2(t), rtol=1e-6)
+    lines = open(os.path.join(out, "U0-final.pos")).read().splitlines()
+    assert lines[0].startswith('View "U0 "') and len(lines) == mesh.K + 2
+    uv = s.eval_u(0)
+    first = [float(x) for x in re.findall(r"\{([^}]*)\}", lines[1])[0].split(",")]
+    np.testing.assert_allclose(first, uv[:, 0], rtol=1e-12)
