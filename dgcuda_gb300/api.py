@@ -102,6 +102,15 @@ def _declare(L):
         "dg_kernel_launches": (C.c_longlong, [C.c_void_p]),
         "dg_measure_fp64_peak": (C.c_int, [C.c_int, _dp]),
         "dg_eval_vertices": (C.c_int, [C.c_void_p, C.c_int, _dp]),
+        "dg_set_bathymetry": (C.c_int, [C.c_void_p, _dp]),
+        "dg_bathymetry_project": (C.c_int, [C.c_void_p, C.c_int, _dp]),
+        "dg_get_bathymetry": (C.c_int, [C.c_void_p, _dp]),
+        "dg_autotune": (C.c_int, [C.c_void_p, _ip]),
+        "dg_batch_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
+        "dg_batch_step": (C.c_int, [C.c_void_p, C.c_int, _dp]),
+        "dg_batch_autotune": (C.c_int, [C.c_void_p, _ip]),
+        "dg_batch_launches": (C.c_longlong, [C.c_void_p]),
+        "dg_batch_destroy": (None, [C.c_void_p]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(L, name, None)
@@ -109,6 +118,41 @@ def _declare(L):
             continue
         fn.restype = res
         fn.argtypes = args
+
+
+class Batch:
+    """Independent problems stepped together (dg_batch): one launch per
+    kernel per RK stage for all members, one CUDA graph per ensemble step."""
+
+    def __init__(self, solvers):
+        self._L = load_library()
+        self.solvers = list(solvers)
+        arr = (C.c_void_p * len(self.solvers))(*[s._h.value for s in self.solvers])
+        h = C.c_void_p()
+        _check(self._L.dg_batch_create(len(self.solvers), arr, C.byref(h)))
+        self._h = h
+
+    def step(self, nsteps, t=None):
+        tt = np.zeros(len(self.solvers)) if t is None else np.array(t, dtype=np.float64)
+        _check(self._L.dg_batch_step(self._h, nsteps, _dptr(tt)))
+        return tt
+
+    def autotune(self):
+        b = C.c_int()
+        _check(self._L.dg_batch_autotune(self._h, C.byref(b)))
+        return b.value
+
+    def launches(self):
+        return self._L.dg_batch_launches(self._h)
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._L.dg_batch_destroy(h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
 
 
 def measure_fp64_peak(device=0):
@@ -291,6 +335,30 @@ class Solver:
         out = np.empty((3, self.K))
         _check(self._L.dg_eval_vertices(self._h, var, _dptr(out)))
         return out
+
+    def set_bathymetry(self, b):
+        """Shallow-water bed modes [mode][elem] (.pmsh order) or None (flat)."""
+        if b is None:
+            _check(self._L.dg_set_bathymetry(self._h, None))
+            return
+        b = np.ascontiguousarray(b, dtype=np.float64).reshape(self.n_p, self.K)
+        _check(self._L.dg_set_bathymetry(self._h, _dptr(b)))
+
+    def get_bathymetry(self):
+        b = np.empty((self.n_p, self.K))
+        _check(self._L.dg_get_bathymetry(self._h, _dptr(b)))
+        return b
+
+    def bathymetry_project(self, kind, prm=(0.0, 0.0, 0.0)):
+        """kind: 'flat', 'sine' (A, kx, ky) or 'linear' (b0, bx, by)."""
+        k = {"flat": 0, "sine": 1, "linear": 2}[kind]
+        a = np.ascontiguousarray(prm, dtype=np.float64)
+        _check(self._L.dg_bathymetry_project(self._h, k, _dptr(a)))
+
+    def autotune(self):
+        b = C.c_int()
+        _check(self._L.dg_autotune(self._h, C.byref(b)))
+        return b.value
 
     def stream(self):
         return self._L.dg_solver_stream(self._h)

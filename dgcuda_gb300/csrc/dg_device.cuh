@@ -9,6 +9,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "dg_launch.h"
 #include "dg_tables_data.h"
 
 #define DG_HD __host__ __device__ __forceinline__
@@ -33,12 +34,6 @@ struct Tab {
   double V[3][NP];       // phi_i at the vertices (0,0), (1,0), (0,1)
 };
 
-// equation / problem parameters (kernel parameter)
-struct EqP {
-  double gamma, g, ax, ay, mu, eps;
-  int problem, pad;
-  double prm[8];
-};
 
 enum Problem {
   PB_NONE = 0, PB_ADV_SINE = 1, PB_ADV_LINEAR = 2, PB_EULER_VORTEX = 3, PB_EULER_RIEMANN4 = 4,
@@ -46,6 +41,16 @@ enum Problem {
 };
 
 constexpr double kPi = 3.141592653589793238462643383279502884;
+
+// a product that is not fused into an FMA with a later add (same rounding in
+// every kernel instance that inlines the caller)
+DG_HD double mul_rn(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __dmul_rn(a, b);
+#else
+  return a * b;
+#endif
+}
 
 // --------------------------------------------------------------------------
 // problem plugins: exact / initial / inflow state (U0, U_exact, U_inflow)
@@ -68,7 +73,7 @@ DG_HD void exact_state(const EqP &q, double *U, double x, double y, double t) {
         dx -= L * floor(dx / L + 0.5);
         dy -= L * floor(dy / L + 0.5);
       }
-      double r2 = dx * dx + dy * dy;
+      double r2 = fma(dx, dx, dy * dy);
       double e = exp(0.5 * (1 - r2));
       double u = P[3] - beta / (2 * kPi) * e * dy;
       double v = P[4] + beta / (2 * kPi) * e * dx;
@@ -78,7 +83,7 @@ DG_HD void exact_state(const EqP &q, double *U, double x, double y, double t) {
       U[0] = rho;
       U[1] = rho * u;
       U[2] = rho * v;
-      U[3] = p / (gam - 1) + 0.5 * rho * (u * u + v * v);
+      U[3] = fma(0.5 * rho, fma(u, u, v * v), p / (gam - 1));
       break;
     }
     case PB_EULER_RIEMANN4: {  // four-quadrant Riemann data split at (0.5, 0.5)
@@ -90,28 +95,28 @@ DG_HD void exact_state(const EqP &q, double *U, double x, double y, double t) {
       U[0] = rho;
       U[1] = rho * u;
       U[2] = rho * v;
-      U[3] = p / (gam - 1) + 0.5 * rho * (u * u + v * v);
+      U[3] = fma(0.5 * rho, fma(u, u, v * v), p / (gam - 1));
       break;
     }
     case PB_EULER_SUPERSONIC: {  // euler/supersonic/supersonic.cu:27-37
       const double GAM = 1.4, MACH = 2.25;
-      double r = sqrt(x * x + y * y);
+      double r = sqrt(fma(x, x, y * y));
       U[0] = pow(1 + 1.0125 * (1. - 1. / (r * r)), 2.5);
       U[1] = U[0] * sin(atan(y / x)) * MACH / r;
       U[2] = U[0] * -cos(atan(y / x)) * MACH / r;
       double p = (1.0 / GAM) * pow(U[0], GAM);
-      U[3] = 0.5 * U[0] * (MACH * MACH / (r * r)) + p * (1. / (GAM - 1.));
+      U[3] = fma(0.5 * U[0], MACH * MACH / (r * r), p * (1. / (GAM - 1.)));
       break;
     }
     case PB_SW_HUMP: {  // still water with a Gaussian hump: h0, A, sigma, x0, y0
       double dx = x - P[3], dy = y - P[4], s = P[2];
-      U[0] = P[0] + P[1] * exp(-(dx * dx + dy * dy) / (s * s));
+      U[0] = fma(P[1], exp(-fma(dx, dx, dy * dy) / (s * s)), P[0]);
       U[1] = 0;
       U[2] = 0;
       break;
     }
     case PB_SW_TEST:  // shallowwater/test/test.cu:25-35
-      U[0] = 10 + exp(-((x - 0.5) * (x - 0.5) + (y - 0.5) * (y - 0.5)) / (2 * 0.1 * 0.1));
+      U[0] = 10 + exp(-fma(x - 0.5, x - 0.5, (y - 0.5) * (y - 0.5)) / (2 * 0.1 * 0.1));
       U[1] = 0;
       U[2] = 0;
       break;
@@ -133,6 +138,7 @@ DG_HD void exact_state(const EqP &q, double *U, double x, double y, double t) {
 // --------------------------------------------------------------------------
 struct Advection {  // advection/advection.cu
   static constexpr int N = 1;
+  static constexpr bool kBathymetry = false;
   DG_HD static bool physical(const EqP &, const double *) { return true; }
   DG_HD static void flux(const EqP &q, const double *U, double *fx, double *fy) {
     fx[0] = q.ax * U[0];
@@ -141,11 +147,11 @@ struct Advection {  // advection/advection.cu
   // upwind flux (riemann_solver_upwind, advection.cu:94-116)
   DG_HD static void riemann(const EqP &q, const double *UL, const double *UR, double nx, double ny,
                             double *F) {
-    double an = nx * q.ax + ny * q.ay;
+    double an = fma(nx, q.ax, ny * q.ay);
     F[0] = an > 0 ? an * UL[0] : an * UR[0];
   }
   DG_HD static double mean_speed(const EqP &q, const double *) {
-    return sqrt(q.ax * q.ax + q.ay * q.ay);
+    return sqrt(fma(q.ax, q.ax, q.ay * q.ay));
   }
   DG_HD static void reflect(const EqP &, const double *, double *UR, double, double, double,
                             double) {
@@ -156,65 +162,70 @@ struct Advection {  // advection/advection.cu
 
 struct Euler {  // euler/euler.cu
   static constexpr int N = 4;
+  static constexpr bool kBathymetry = false;
   // rho >= 0 and p >= 0 (is_physical, euler.cu:76-86); with rho > 0,
   // p < 0 <=> 2 rho E < |rho u|^2, which needs no FP64 division
   DG_HD static bool physical(const EqP &, const double *U) {
     if (U[0] < 0) return false;
-    return !(2.0 * U[0] * U[3] < U[1] * U[1] + U[2] * U[2]);
+    return !(2.0 * U[0] * U[3] < fma(U[1], U[1], U[2] * U[2]));
   }
   DG_HD static void flux(const EqP &q, const double *U, double *fx, double *fy) {
     double ir = 1.0 / U[0];
     double u = U[1] * ir, v = U[2] * ir;
-    double p = (q.gamma - 1.) * (U[3] - 0.5 * (U[1] * u + U[2] * v));
+    // p is reused as an addend: round it explicitly (never fused into an FMA)
+    double p = mul_rn(q.gamma - 1., fma(-0.5, fma(U[1], u, U[2] * v), U[3]));
     double H = U[3] + p;
     fx[0] = U[1];
-    fx[1] = U[1] * u + p;
+    fx[1] = fma(U[1], u, p);
     fx[2] = U[2] * u;
     fx[3] = H * u;
     fy[0] = U[2];
     fy[1] = U[1] * v;
-    fy[2] = U[2] * v + p;
+    fy[2] = fma(U[2], v, p);
     fy[3] = H * v;
   }
   // local Lax-Friedrichs (euler.cu:170-237)
   DG_HD static void riemann(const EqP &q, const double *UL, const double *UR, double nx, double ny,
                             double *F) {
+    // every multiply-add is an explicit fma so the rounding does not depend
+    // on how the compiler contracts the expression in a given kernel
     double irl = 1.0 / UL[0], irr = 1.0 / UR[0];
     double ul = UL[1] * irl, vl = UL[2] * irl, ur = UR[1] * irr, vr = UR[2] * irr;
-    double pl = (q.gamma - 1.) * (UL[3] - 0.5 * (UL[1] * ul + UL[2] * vl));
-    double pr = (q.gamma - 1.) * (UR[3] - 0.5 * (UR[1] * ur + UR[2] * vr));
-    double snl = nx * ul + ny * vl, snr = nx * ur + ny * vr;
+    double pl = mul_rn(q.gamma - 1., fma(-0.5, fma(UL[1], ul, UL[2] * vl), UL[3]));
+    double pr = mul_rn(q.gamma - 1., fma(-0.5, fma(UR[1], ur, UR[2] * vr), UR[3]));
+    double snl = fma(nx, ul, ny * vl), snr = fma(nx, ur, ny * vr);
     double cl = sqrt(q.gamma * pl * irl), cr = sqrt(q.gamma * pr * irr);
     double lam = fmax(fabs(snl) + cl, fabs(snr) + cr);
-    double fl0 = UL[0] * snl, fr0 = UR[0] * snr;
-    F[0] = 0.5 * (fl0 + fr0 + lam * (UL[0] - UR[0]));
-    F[1] = 0.5 * (UL[1] * snl + pl * nx + UR[1] * snr + pr * nx + lam * (UL[1] - UR[1]));
-    F[2] = 0.5 * (UL[2] * snl + pl * ny + UR[2] * snr + pr * ny + lam * (UL[2] - UR[2]));
-    F[3] = 0.5 * ((UL[3] + pl) * snl + (UR[3] + pr) * snr + lam * (UL[3] - UR[3]));
+    F[0] = 0.5 * fma(lam, UL[0] - UR[0], fma(UL[0], snl, UR[0] * snr));
+    F[1] = 0.5 * fma(lam, UL[1] - UR[1], fma(UL[1], snl, fma(pl, nx, fma(UR[1], snr, pr * nx))));
+    F[2] = 0.5 * fma(lam, UL[2] - UR[2], fma(UL[2], snl, fma(pl, ny, fma(UR[2], snr, pr * ny))));
+    F[3] = 0.5 * fma(lam, UL[3] - UR[3], fma(UL[3] + pl, snl, (UR[3] + pr) * snr));
   }
   DG_HD static double mean_speed(const EqP &q, const double *U) {  // euler.cu:248-277
-    double p = (q.gamma - 1.) * (U[3] - (U[1] * U[1] + U[2] * U[2]) / 2. / U[0]);
+    const double m2 = fma(U[1], U[1], U[2] * U[2]);
+    double p = (q.gamma - 1.) * (U[3] - m2 / 2. / U[0]);
     double c = sqrt(q.gamma * p / U[0]);
-    double s = sqrt(U[1] * U[1] + U[2] * U[2]) / U[0];
+    double s = sqrt(m2) / U[0];
     return s > 0 ? s + c : -s + c;
   }
   DG_HD static void reflect(const EqP &q, const double *UL, double *UR, double x, double y,
                             double nx, double ny) {
     if (q.problem == PB_EULER_SUPERSONIC) {  // supersonic.cu:65-87, curved wall
-      double d = sqrt(x * x + y * y), Nx = x / d, Ny = y / d;
+      double d = sqrt(fma(x, x, y * y)), Nx = x / d, Ny = y / d;
       if (Nx * nx + Ny * ny < 0) {
         Nx = -Nx;
         Ny = -Ny;
       }
       UR[0] = UL[0];
       UR[3] = UL[3];
-      UR[1] = (UL[1] * Ny - UL[2] * Nx) * Ny;
-      UR[2] = -(UL[1] * Ny - UL[2] * Nx) * Nx;
+      const double tg = fma(UL[1], Ny, -UL[2] * Nx);
+      UR[1] = tg * Ny;
+      UR[2] = -tg * Nx;
     } else {  // slip wall: mirror the momentum
-      double dot = UL[1] * nx + UL[2] * ny;
+      double dot = fma(UL[1], nx, UL[2] * ny);
       UR[0] = UL[0];
-      UR[1] = UL[1] - 2 * dot * nx;
-      UR[2] = UL[2] - 2 * dot * ny;
+      UR[1] = fma(-2 * dot, nx, UL[1]);
+      UR[2] = fma(-2 * dot, ny, UL[2]);
       UR[3] = UL[3];
     }
   }
@@ -223,45 +234,47 @@ struct Euler {  // euler/euler.cu
 
 struct ShallowWater {  // shallowwater/shallowwater.cu (g is a parameter here)
   static constexpr int N = 3;
+  static constexpr bool kBathymetry = true;  // optional bed b(x, y): source -g h grad b
   DG_HD static bool physical(const EqP &, const double *U) { return U[0] >= 0.; }
   DG_HD static void flux(const EqP &q, const double *U, double *fx, double *fy) {
     double ih = 1.0 / U[0];
     double u = U[1] * ih, v = U[2] * ih, hp = 0.5 * q.g * U[0] * U[0];
     fx[0] = U[1];
-    fx[1] = U[1] * u + hp;
+    fx[1] = fma(U[1], u, hp);
     fx[2] = U[2] * u;
     fy[0] = U[2];
     fy[1] = U[1] * v;
-    fy[2] = U[2] * v + hp;
+    fy[2] = fma(U[2], v, hp);
   }
   DG_HD static void riemann(const EqP &q, const double *UL, const double *UR, double nx, double ny,
                             double *F) {  // shallowwater.cu:118-185
     double ihl = 1.0 / UL[0], ihr = 1.0 / UR[0];
-    double snl = (nx * UL[1] + ny * UL[2]) * ihl, snr = (nx * UR[1] + ny * UR[2]) * ihr;
+    double snl = fma(nx, UL[1], ny * UL[2]) * ihl, snr = fma(nx, UR[1], ny * UR[2]) * ihr;
     double cl = sqrt(UL[0] * q.g), cr = sqrt(UR[0] * q.g);
     double lam = fmax(fabs(snl) + cl, fabs(snr) + cr);
     double pl = 0.5 * q.g * UL[0] * UL[0], pr = 0.5 * q.g * UR[0] * UR[0];
-    F[0] = 0.5 * (UL[0] * snl + UR[0] * snr + lam * (UL[0] - UR[0]));
-    F[1] = 0.5 * (UL[1] * snl + pl * nx + UR[1] * snr + pr * nx + lam * (UL[1] - UR[1]));
-    F[2] = 0.5 * (UL[2] * snl + pl * ny + UR[2] * snr + pr * ny + lam * (UL[2] - UR[2]));
+    F[0] = 0.5 * fma(lam, UL[0] - UR[0], fma(UL[0], snl, UR[0] * snr));
+    F[1] = 0.5 * fma(lam, UL[1] - UR[1], fma(UL[1], snl, fma(pl, nx, fma(UR[1], snr, pr * nx))));
+    F[2] = 0.5 * fma(lam, UL[2] - UR[2], fma(UL[2], snl, fma(pl, ny, fma(UR[2], snr, pr * ny))));
   }
   DG_HD static double mean_speed(const EqP &q, const double *U) {  // shallowwater.cu:196-224
     double c = sqrt(U[0] * q.g);
-    double s = sqrt(U[1] * U[1] + U[2] * U[2]) / U[0];
+    double s = sqrt(fma(U[1], U[1], U[2] * U[2])) / U[0];
     return s > 0 ? s + c : -s + c;
   }
   DG_HD static void reflect(const EqP &, const double *UL, double *UR, double, double, double nx,
                             double ny) {  // shallowwater/test/test.cu:63-77
-    double dot = UL[1] * nx + UL[2] * ny;
+    double dot = fma(UL[1], nx, UL[2] * ny);
     UR[0] = UL[0];
-    UR[1] = UL[1] - 2 * dot * nx;
-    UR[2] = UL[2] - 2 * dot * ny;
+    UR[1] = fma(-2 * dot, nx, UL[1]);
+    UR[2] = fma(-2 * dot, ny, UL[2]);
   }
   static constexpr bool outflow_uses_exact = false;
 };
 
 struct Maxwell {  // maxwells/maxwells.cu, U = (Hx, Hy, Ez)
   static constexpr int N = 3;
+  static constexpr bool kBathymetry = false;
   DG_HD static bool physical(const EqP &, const double *) { return true; }
   DG_HD static void flux(const EqP &q, const double *U, double *fx, double *fy) {
     double imu = 1. / q.mu, ieps = 1. / q.eps;
@@ -276,17 +289,17 @@ struct Maxwell {  // maxwells/maxwells.cu, U = (Hx, Hy, Ez)
                             double *F) {  // maxwells.cu:93-163, LLF with lambda = 1/sqrt(eps mu)
     double imu = 1. / q.mu, ieps = 1. / q.eps, lam = fabs(1. / sqrt(q.eps * q.mu));
     double ez = UL[2] + UR[2], hx = UL[0] + UR[0], hy = UL[1] + UR[1];
-    F[0] = 0.5 * (-imu * ez * ny + lam * (UL[0] - UR[0]));
-    F[1] = 0.5 * (imu * ez * nx + lam * (UL[1] - UR[1]));
-    F[2] = 0.5 * (ieps * (hy * nx - hx * ny) + lam * (UL[2] - UR[2]));
+    F[0] = 0.5 * fma(lam, UL[0] - UR[0], -imu * ez * ny);
+    F[1] = 0.5 * fma(lam, UL[1] - UR[1], imu * ez * nx);
+    F[2] = 0.5 * fma(lam, UL[2] - UR[2], ieps * fma(hy, nx, -hx * ny));
   }
   DG_HD static double mean_speed(const EqP &q, const double *) { return fabs(1. / sqrt(q.eps * q.mu)); }
   DG_HD static void reflect(const EqP &, const double *UL, double *UR, double, double, double nx,
                             double ny) {  // maxwells/cmirror/cmirror.cu:63-77
-    double dot = UL[0] * nx + UL[1] * ny;
+    double dot = fma(UL[0], nx, UL[1] * ny);
     UR[2] = UL[2];
-    UR[0] = UL[0] - 2 * dot * nx;
-    UR[1] = UL[1] - 2 * dot * ny;
+    UR[0] = fma(-2 * dot, nx, UL[0]);
+    UR[1] = fma(-2 * dot, ny, UL[1]);
   }
   static constexpr bool outflow_uses_exact = false;
 };

@@ -40,7 +40,8 @@
 
 namespace dg {
 
-constexpr int kBlock = 128;
+constexpr int kBlock = 128;     // fixed block of the auxiliary kernels
+constexpr int kMaxBlock = 256;  // largest autotuned block of the stage kernels
 
 template <int P>
 __device__ __forceinline__ size_t trace_stride() {
@@ -49,12 +50,9 @@ __device__ __forceinline__ size_t trace_stride() {
 
 // ---------------------------------------------------------------------------
 template <class Eq, int P>
-__global__ void __launch_bounds__(kBlock) k_trace(const __grid_constant__ Tab<P> tab,
-                                                  const __grid_constant__ EqP q, double *u,
-                                                  double *__restrict__ T, int K, int Kp) {
+__device__ __forceinline__ void trace_body(const Tab<P> &tab, const EqP &q, double *u,
+                                           double *__restrict__ T, int Kp, int e) {
   constexpr int N = Eq::N, NP = Tab<P>::NP, N1 = Tab<P>::N1;
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= K) return;
   double c[N][NP];
 #pragma unroll
   for (int n = 0; n < N; n++)
@@ -91,25 +89,36 @@ __global__ void __launch_bounds__(kBlock) k_trace(const __grid_constant__ Tab<P>
   }
 }
 
-// ---------------------------------------------------------------------------
 template <class Eq, int P>
-__global__ void __launch_bounds__(kBlock) k_face(const __grid_constant__ Tab<P> tab,
-                                                 const __grid_constant__ EqP q,
-                                                 const double *__restrict__ T,
-                                                 const int4 *__restrict__ side,
-                                                 const double *__restrict__ sgeo,
-                                                 const double *__restrict__ bxy,
-                                                 double *__restrict__ Fh, const double *tptr,
-                                                 const double *dtp, double tcoef, int S, int Sb) {
+__global__ void __launch_bounds__(kMaxBlock) k_trace(const __grid_constant__ Tab<P> tab,
+                                                     const __grid_constant__ EqP q, double *u,
+                                                     double *__restrict__ T, int K, int Kp) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < K) trace_body<Eq, P>(tab, q, u, T, Kp, e);
+}
+
+// ---------------------------------------------------------------------------
+struct FaceArgs {
+  const double *T;
+  const int4 *side;
+  const double *sgeo, *bxy;
+  double *Fh;
+  const double *tptr, *dtp;
+  double tcoef;
+  int S, Sb;
+};
+
+template <class Eq, int P>
+__device__ __forceinline__ void face_body(const Tab<P> &tab, const EqP &q, const FaceArgs &a,
+                                          int s) {
   constexpr int N = Eq::N, N1 = P + 1;
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= S) return;
-  const int4 sd = side[s];
-  const double nx = sgeo[s], ny = sgeo[S + s], hl = sgeo[2 * (size_t)S + s];
-  const double *TL = T + ((size_t)sd.x * 3 + sd.z) * (N1 * N);
-  double *F = Fh + (size_t)s * (N1 * N);
+  const int S = a.S, Sb = a.Sb;
+  const int4 sd = a.side[s];
+  const double nx = a.sgeo[s], ny = a.sgeo[S + s], hl = a.sgeo[2 * (size_t)S + s];
+  const double *TL = a.T + ((size_t)sd.x * 3 + sd.z) * (N1 * N);
+  double *F = a.Fh + (size_t)s * (N1 * N);
   if (sd.y >= 0) {
-    const double *TR = T + ((size_t)sd.y * 3 + sd.w) * (N1 * N);
+    const double *TR = a.T + ((size_t)sd.y * 3 + sd.w) * (N1 * N);
 #pragma unroll
     for (int j = 0; j < N1; j++) {
       double UL[N], UR[N], Fn[N];
@@ -124,7 +133,8 @@ __global__ void __launch_bounds__(kBlock) k_face(const __grid_constant__ Tab<P> 
       for (int n = 0; n < N; n++) F[j * N + n] = Fn[n] * sc;
     }
   } else {
-    const double t = *tptr + tcoef * *dtp;
+    const double t = *a.tptr + a.tcoef * *a.dtp;
+    const double *bxy = a.bxy;
     const double xa = bxy[s], ya = bxy[Sb + s], xb = bxy[2 * Sb + s], yb = bxy[3 * Sb + s];
 #pragma unroll
     for (int j = 0; j < N1; j++) {
@@ -132,13 +142,21 @@ __global__ void __launch_bounds__(kBlock) k_face(const __grid_constant__ Tab<P> 
 #pragma unroll
       for (int n = 0; n < N; n++) UL[n] = TL[j * N + n];
       const double r = 0.5 + 0.5 * tab.t1[j];
-      ghost_state<Eq>(q, sd.y, UL, UR, xa + r * (xb - xa), ya + r * (yb - ya), t, nx, ny);
+      ghost_state<Eq>(q, sd.y, UL, UR, fma(r, xb - xa, xa), fma(r, yb - ya, ya), t, nx, ny);
       Eq::riemann(q, UL, UR, nx, ny, Fn);
       const double sc = hl * tab.w1[j];
 #pragma unroll
       for (int n = 0; n < N; n++) F[j * N + n] = Fn[n] * sc;
     }
   }
+}
+
+template <class Eq, int P>
+__global__ void __launch_bounds__(kMaxBlock) k_face(const __grid_constant__ Tab<P> tab,
+                                                    const __grid_constant__ EqP q,
+                                                    const __grid_constant__ FaceArgs a) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < a.S) face_body<Eq, P>(tab, q, a, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -148,7 +166,7 @@ template <class Eq, int P>
 __device__ __forceinline__ bool volume(const Tab<P> &tab, const EqP &q,
                                        const double (&c)[Eq::N][Tab<P>::NP],
                                        double (&acc)[Eq::N][Tab<P>::NP], double xr, double yr,
-                                       double xs, double ys) {
+                                       double xs, double ys, const double *bz) {
   constexpr int N = Eq::N, NP = Tab<P>::NP, NQ = Tab<P>::NQ;
   bool ok = true;
 #pragma unroll
@@ -172,22 +190,52 @@ __device__ __forceinline__ bool volume(const Tab<P> &tab, const EqP &q,
       for (int i = 1; i < NP; i++)  // grad phi_0 = 0
         acc[n][i] = fma(tab.GR[k][i], gr, fma(tab.GS[k][i], gs, acc[n][i]));
     }
+    if (Eq::kBathymetry && bz) {
+      // bed slope source S = (0, -g h b_x, -g h b_y) (the reference's
+      // source_term hook, eval_volume :1063-1079): w_q J S projected on
+      // phi_i, with w_q J grad b from the weighted gradient tables
+      double br = 0.0, bs = 0.0;
+#pragma unroll
+      for (int i = 1; i < NP; i++) {
+        br = fma(bz[i], tab.GR[k][i], br);
+        bs = fma(bz[i], tab.GS[k][i], bs);
+      }
+      const double gh = -q.g * U[0];
+      const double sx = gh * fma(ys, br, -yr * bs), sy = gh * fma(xr, bs, -xs * br);
+#pragma unroll
+      for (int i = 0; i < NP; i++) {
+        acc[1][i] = fma(sx, tab.B[k][i], acc[1][i]);
+        acc[2][i] = fma(sy, tab.B[k][i], acc[2][i]);
+      }
+    }
   }
   return ok;
 }
+
+// arguments of one element-kernel launch on one problem
+struct ElemArgs {
+  double *us;               // stage input (flattened in place if needed)
+  const double *un;         // u^n for the RK combination (ca != 0)
+  double *out;              // stage output; may alias us or un
+  const double *Fh;         // side fluxes
+  const int *esd;           // sides of each element
+  const double *geo;        // metric
+  const double *dtp;        // time step
+  const double *bathy;      // bed modes [mode][Kp] (shallow water) or null
+  double *T;                // traces of out (TR)
+  double ca, cb, cc;
+  int K, Kp, check;
+};
 
 // TR: also write the edge traces of `out` into T (what k_trace would compute
 // from it at the start of the next stage, bit for bit) and, when `check` is
 // set, flatten an element whose new traces are non-physical
 template <class Eq, int P, bool TR>
-__global__ void __launch_bounds__(kBlock) k_element(
-    const __grid_constant__ Tab<P> tab, const __grid_constant__ EqP q, double *us,
-    const double *un, double *out, const double *__restrict__ Fh, const int *__restrict__ esd,
-    const double *__restrict__ geo, const double *dtp, double ca, double cb, double cc, int K,
-    int Kp, double *__restrict__ T, int check) {
+__device__ __forceinline__ void element_body(const Tab<P> &tab, const EqP &q, const ElemArgs &a,
+                                             int e) {
   constexpr int N = Eq::N, NP = Tab<P>::NP, N1 = Tab<P>::N1;
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= K) return;
+  const int Kp = a.Kp;
+  double *us = a.us, *out = a.out;
   double c[N][NP], acc[N][NP];
 #pragma unroll
   for (int n = 0; n < N; n++)
@@ -196,9 +244,18 @@ __global__ void __launch_bounds__(kBlock) k_element(
       c[n][i] = us[(size_t)(n * NP + i) * Kp + e];
       acc[n][i] = 0.0;
     }
+  const double *geo = a.geo;
   const double xr = geo[e], yr = geo[(size_t)Kp + e], xs = geo[2 * (size_t)Kp + e],
                ys = geo[3 * (size_t)Kp + e], iJ = geo[4 * (size_t)Kp + e];
-  if (!volume<Eq, P>(tab, q, c, acc, xr, yr, xs, ys)) {
+  double bz[Eq::kBathymetry ? NP : 1];
+  const bool has_b = Eq::kBathymetry && a.bathy;
+  if (Eq::kBathymetry) {
+#pragma unroll
+    for (int i = 0; i < (Eq::kBathymetry ? NP : 1); i++)
+      bz[i] = has_b ? a.bathy[(size_t)i * Kp + e] : 0.0;
+  }
+  const double *bzp = has_b ? bz : nullptr;
+  if (!volume<Eq, P>(tab, q, c, acc, xr, yr, xs, ys, bzp)) {
     // non-physical volume value: the element's mean replaces it everywhere
 #pragma unroll
     for (int n = 0; n < N; n++)
@@ -207,7 +264,7 @@ __global__ void __launch_bounds__(kBlock) k_element(
         acc[n][i] = 0.0;
         if (i > 0) c[n][i] = 0.0;
       }
-    volume<Eq, P>(tab, q, c, acc, xr, yr, xs, ys);
+    volume<Eq, P>(tab, q, c, acc, xr, yr, xs, ys, bzp);
     if (us != out)
 #pragma unroll
       for (int n = 0; n < N; n++)
@@ -217,9 +274,9 @@ __global__ void __launch_bounds__(kBlock) k_element(
   // surface: -F on a left face, +F (mirrored points) on a right face
 #pragma unroll
   for (int f = 0; f < 3; f++) {
-    const int sd = esd[(size_t)f * Kp + e];
+    const int sd = a.esd[(size_t)f * Kp + e];
     const bool right = sd & 1;
-    const double *F = Fh + (size_t)(sd >> 1) * (N1 * N);
+    const double *F = a.Fh + (size_t)(sd >> 1) * (N1 * N);
     const double sg = right ? 1.0 : -1.0;
 #pragma unroll
     for (int j = 0; j < N1; j++) {
@@ -232,20 +289,20 @@ __global__ void __launch_bounds__(kBlock) k_element(
       }
     }
   }
-  const double dt = *dtp;
-  const double s = cc * dt * iJ;
+  const double dt = *a.dtp;
+  const double s = a.cc * dt * iJ;
 #pragma unroll
   for (int n = 0; n < N; n++)
 #pragma unroll
     for (int i = 0; i < NP; i++) {
       const size_t o = (size_t)(n * NP + i) * Kp + e;
-      double v = fma(s, acc[n][i], cb * c[n][i]);
-      if (ca != 0.0) v = fma(ca, un[o], v);
+      double v = fma(s, acc[n][i], a.cb * c[n][i]);
+      if (a.ca != 0.0) v = fma(a.ca, a.un[o], v);
       out[o] = v;
       if (TR) acc[n][i] = v;
     }
   if (TR) {
-    double *Te = T + (size_t)e * (3 * N1 * N);
+    double *Te = a.T + (size_t)e * (3 * N1 * N);
     bool bad = false;
 #pragma unroll
     for (int f = 0; f < 3; f++)
@@ -254,16 +311,16 @@ __global__ void __launch_bounds__(kBlock) k_element(
         double U[N];
 #pragma unroll
         for (int n = 0; n < N; n++) {
-          double a = acc[n][0] * tab.E[f][j][0];
+          double v = acc[n][0] * tab.E[f][j][0];
 #pragma unroll
-          for (int i = 1; i < NP; i++) a = fma(acc[n][i], tab.E[f][j][i], a);
-          U[n] = a;
+          for (int i = 1; i < NP; i++) v = fma(acc[n][i], tab.E[f][j][i], v);
+          U[n] = v;
         }
         bad |= !Eq::physical(q, U);
 #pragma unroll
         for (int n = 0; n < N; n++) Te[(f * N1 + j) * N + n] = U[n];
       }
-    if (check && bad) {
+    if (a.check && bad) {
 #pragma unroll
       for (int n = 0; n < N; n++) {
 #pragma unroll
@@ -277,9 +334,17 @@ __global__ void __launch_bounds__(kBlock) k_element(
   }
 }
 
+template <class Eq, int P, bool TR>
+__global__ void __launch_bounds__(kMaxBlock) k_element(const __grid_constant__ Tab<P> tab,
+                                                       const __grid_constant__ EqP q,
+                                                       const __grid_constant__ ElemArgs a) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < a.K) element_body<Eq, P, TR>(tab, q, a, e);
+}
+
 // ---------------------------------------------------------------------------
 template <class Eq, int P>
-__global__ void __launch_bounds__(kBlock) k_limit(const __grid_constant__ Tab<P> tab,
+__global__ void __launch_bounds__(kMaxBlock) k_limit(const __grid_constant__ Tab<P> tab,
                                                   double *u, const int *__restrict__ nbr,
                                                   int K, int Kp) {
   constexpr int N = Eq::N, NP = Tab<P>::NP, N1 = Tab<P>::N1;
@@ -293,8 +358,11 @@ __global__ void __launch_bounds__(kBlock) k_limit(const __grid_constant__ Tab<P>
     double c[NP];
 #pragma unroll
     for (int i = 0; i < NP; i++) c[i] = row[(size_t)i * Kp + e];
-    const double Uc = c[0] * phi0;
-    const double m0 = row[nb0] * phi0, m1 = row[nb1] * phi0, m2 = row[nb2] * phi0;
+    // products reused as addends are rounded explicitly (__dmul_rn is never
+    // fused into an FMA), so every kernel instance rounds them the same way
+    const double Uc = __dmul_rn(c[0], phi0);
+    const double m0 = __dmul_rn(row[nb0], phi0), m1 = __dmul_rn(row[nb1], phi0),
+                 m2 = __dmul_rn(row[nb2], phi0);
     const double Umin = fmin(Uc, fmin(m0, fmin(m1, m2)));
     const double Umax = fmax(Uc, fmax(m0, fmax(m1, m2)));
     // largest overshoot above / below the mean over the edge points; the
@@ -334,14 +402,10 @@ __global__ void __launch_bounds__(kBlock) k_limit(const __grid_constant__ Tab<P>
 // traces.  T ends up holding exactly what k_trace would compute from the
 // limited state.
 template <class Eq, int P>
-__global__ void __launch_bounds__(kBlock) k_limit_tr(const __grid_constant__ Tab<P> tab,
-                                                     const __grid_constant__ EqP q, double *u,
-                                                     double *__restrict__ T,
-                                                     const int *__restrict__ nbr, int K,
-                                                     int Kp) {
+__device__ __forceinline__ void limit_tr_body(const Tab<P> &tab, const EqP &q, double *u,
+                                              double *__restrict__ T,
+                                              const int *__restrict__ nbr, int Kp, int e) {
   constexpr int N = Eq::N, NP = Tab<P>::NP, N1 = Tab<P>::N1;
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= K) return;
   const int nb0 = nbr[e], nb1 = nbr[(size_t)Kp + e], nb2 = nbr[2 * (size_t)Kp + e];
   const double phi0 = tab.B[0][0];
   double *Te = T + (size_t)e * (3 * N1 * N);
@@ -351,8 +415,11 @@ __global__ void __launch_bounds__(kBlock) k_limit_tr(const __grid_constant__ Tab
   for (int n = 0; n < N; n++) {
     double *row = u + (size_t)(n * NP) * Kp;
     c0[n] = row[e];
-    const double Uc = c0[n] * phi0;
-    const double m0 = row[nb0] * phi0, m1 = row[nb1] * phi0, m2 = row[nb2] * phi0;
+    // products reused as addends are rounded explicitly (__dmul_rn is never
+    // fused into an FMA), so every kernel instance rounds them the same way
+    const double Uc = __dmul_rn(c0[n], phi0);
+    const double m0 = __dmul_rn(row[nb0], phi0), m1 = __dmul_rn(row[nb1], phi0),
+                 m2 = __dmul_rn(row[nb2], phi0);
     const double Umin = fmin(Uc, fmin(m0, fmin(m1, m2)));
     const double Umax = fmax(Uc, fmax(m0, fmax(m1, m2)));
     double up = 0.0, dn = 0.0;
@@ -403,14 +470,24 @@ __global__ void __launch_bounds__(kBlock) k_limit_tr(const __grid_constant__ Tab
   }
 }
 
-// ---------------------------------------------------------------------------
 template <class Eq, int P>
-__global__ void __launch_bounds__(kBlock) k_lambda(const __grid_constant__ Tab<P> tab,
-                                                   const __grid_constant__ EqP q,
-                                                   const double *__restrict__ u, DevScalars *ds,
-                                                   int K, int Kp) {
-  constexpr int N = Eq::N, NP = Tab<P>::NP;
+__global__ void __launch_bounds__(kMaxBlock) k_limit_tr(const __grid_constant__ Tab<P> tab,
+                                                        const __grid_constant__ EqP q,
+                                                        double *u, double *__restrict__ T,
+                                                        const int *__restrict__ nbr, int K,
+                                                        int Kp) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < K) limit_tr_body<Eq, P>(tab, q, u, T, nbr, Kp, e);
+}
+
+// ---------------------------------------------------------------------------
+// block max of the cell-mean wave speed of elements [e0, e0 + blockDim) into
+// ds->lam_bits (the block's elements belong to one problem)
+template <class Eq, int P>
+__device__ __forceinline__ void lambda_body(const Tab<P> &tab, const EqP &q,
+                                            const double *__restrict__ u, DevScalars *ds, int K,
+                                            int Kp, int e) {
+  constexpr int N = Eq::N, NP = Tab<P>::NP;
   double lam = 0.0;
   if (e < K) {
     double U[N];
@@ -432,6 +509,14 @@ __global__ void __launch_bounds__(kBlock) k_lambda(const __grid_constant__ Tab<P
     for (int w = 1; w < kBlock / 32; w++) m = fmax(m, sm[w]);
     atomicMax(&ds->lam_bits, (unsigned long long)__double_as_longlong(m));
   }
+}
+
+template <class Eq, int P>
+__global__ void __launch_bounds__(kBlock) k_lambda(const __grid_constant__ Tab<P> tab,
+                                                   const __grid_constant__ EqP q,
+                                                   const double *__restrict__ u, DevScalars *ds,
+                                                   int K, int Kp) {
+  lambda_body<Eq, P>(tab, q, u, ds, K, Kp, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -538,9 +623,131 @@ __global__ void __launch_bounds__(kBlock) k_vertex(const __grid_constant__ Tab<P
 }
 
 // ---------------------------------------------------------------------------
+// batched kernels: one launch covers every problem of an ensemble.  Block b
+// belongs to problem blk2prob[b] (each problem's elements, or sides, start a
+// fresh block), and runs the same per-element body as the single-problem
+// kernel, with that problem's arrays, parameters and order p in {1, 2, 3}.
+// SSP-RK3 stage st: 0: W = U + dt L(U); 1: W = 3/4 U + 1/4 (W + dt L(W));
+// 2: U = 1/3 U + 2/3 (W + dt L(W)).
+// ---------------------------------------------------------------------------
+struct BatchTabs {
+  Tab<1> t1;
+  Tab<2> t2;
+  Tab<3> t3;
+};
+
+__device__ __forceinline__ ElemArgs batch_elem_args(const BatchProb &pr, int stage, int check) {
+  ElemArgs a;
+  a.us = stage == 0 ? pr.U : pr.W;
+  a.un = pr.U;
+  a.out = stage == 2 ? pr.U : pr.W;
+  a.Fh = pr.Fh;
+  a.esd = pr.esd;
+  a.geo = pr.geo;
+  a.dtp = &pr.ds->dt;
+  a.bathy = pr.bathy;
+  a.T = pr.T;
+  a.ca = stage == 0 ? 0.0 : stage == 1 ? 0.75 : 1.0 / 3.0;
+  a.cb = stage == 0 ? 1.0 : stage == 1 ? 0.25 : 2.0 / 3.0;
+  a.cc = stage == 0 ? 1.0 : stage == 1 ? 0.25 : 2.0 / 3.0;
+  a.K = pr.K;
+  a.Kp = pr.Kp;
+  a.check = check;
+  return a;
+}
+
+template <class Eq>
+__global__ void __launch_bounds__(kMaxBlock)
+    k_element_batch(const __grid_constant__ BatchTabs tb, const BatchProb *__restrict__ probs,
+                    const int *__restrict__ blk2prob, const int *__restrict__ blk0, int stage,
+                    int check) {
+  const int pi = blk2prob[blockIdx.x];
+  const BatchProb &pr = probs[pi];
+  const int e = (blockIdx.x - blk0[pi]) * blockDim.x + threadIdx.x;
+  if (e >= pr.K) return;
+  const ElemArgs a = batch_elem_args(pr, stage, check);
+  switch (pr.p) {
+    case 1: element_body<Eq, 1, true>(tb.t1, pr.q, a, e); break;
+    case 2: element_body<Eq, 2, true>(tb.t2, pr.q, a, e); break;
+    case 3: element_body<Eq, 3, true>(tb.t3, pr.q, a, e); break;
+  }
+}
+
+template <class Eq>
+__global__ void __launch_bounds__(kMaxBlock)
+    k_face_batch(const __grid_constant__ BatchTabs tb, const BatchProb *__restrict__ probs,
+                 const int *__restrict__ blk2prob, const int *__restrict__ blk0, double tcoef) {
+  const int pi = blk2prob[blockIdx.x];
+  const BatchProb &pr = probs[pi];
+  const int s = (blockIdx.x - blk0[pi]) * blockDim.x + threadIdx.x;
+  if (s >= pr.S) return;
+  FaceArgs a;
+  a.T = pr.T;
+  a.side = pr.side;
+  a.sgeo = pr.sgeo;
+  a.bxy = pr.bxy;
+  a.Fh = pr.Fh;
+  a.tptr = &pr.ds->t;
+  a.dtp = &pr.ds->dt;
+  a.tcoef = tcoef;
+  a.S = pr.S;
+  a.Sb = pr.Sb;
+  switch (pr.p) {
+    case 1: face_body<Eq, 1>(tb.t1, pr.q, a, s); break;
+    case 2: face_body<Eq, 2>(tb.t2, pr.q, a, s); break;
+    case 3: face_body<Eq, 3>(tb.t3, pr.q, a, s); break;
+  }
+}
+
+template <class Eq>
+__global__ void __launch_bounds__(kMaxBlock)
+    k_limit_tr_batch(const __grid_constant__ BatchTabs tb, const BatchProb *__restrict__ probs,
+                     const int *__restrict__ blk2prob, const int *__restrict__ blk0, int stage) {
+  const int pi = blk2prob[blockIdx.x];
+  const BatchProb &pr = probs[pi];
+  const int e = (blockIdx.x - blk0[pi]) * blockDim.x + threadIdx.x;
+  if (e >= pr.K) return;
+  double *u = stage == 2 ? pr.U : pr.W;
+  switch (pr.p) {
+    case 1: limit_tr_body<Eq, 1>(tb.t1, pr.q, u, pr.T, pr.nbr, pr.Kp, e); break;
+    case 2: limit_tr_body<Eq, 2>(tb.t2, pr.q, u, pr.T, pr.nbr, pr.Kp, e); break;
+    case 3: limit_tr_body<Eq, 3>(tb.t3, pr.q, u, pr.T, pr.nbr, pr.Kp, e); break;
+  }
+}
+
+template <class Eq>
+__global__ void __launch_bounds__(kMaxBlock)
+    k_trace_batch(const __grid_constant__ BatchTabs tb, const BatchProb *__restrict__ probs,
+                  const int *__restrict__ blk2prob, const int *__restrict__ blk0) {
+  const int pi = blk2prob[blockIdx.x];
+  const BatchProb &pr = probs[pi];
+  const int e = (blockIdx.x - blk0[pi]) * blockDim.x + threadIdx.x;
+  if (e >= pr.K) return;
+  switch (pr.p) {
+    case 1: trace_body<Eq, 1>(tb.t1, pr.q, pr.U, pr.T, pr.Kp, e); break;
+    case 2: trace_body<Eq, 2>(tb.t2, pr.q, pr.U, pr.T, pr.Kp, e); break;
+    case 3: trace_body<Eq, 3>(tb.t3, pr.q, pr.U, pr.T, pr.Kp, e); break;
+  }
+}
+
+template <class Eq>
+__global__ void __launch_bounds__(kBlock)
+    k_lambda_batch(const __grid_constant__ BatchTabs tb, const BatchProb *__restrict__ probs,
+                   const int *__restrict__ blk2prob, const int *__restrict__ blk0) {
+  const int pi = blk2prob[blockIdx.x];
+  const BatchProb &pr = probs[pi];
+  const int e = (blockIdx.x - blk0[pi]) * blockDim.x + threadIdx.x;
+  switch (pr.p) {
+    case 1: lambda_body<Eq, 1>(tb.t1, pr.q, pr.U, pr.ds, pr.K, pr.Kp, e); break;
+    case 2: lambda_body<Eq, 2>(tb.t2, pr.q, pr.U, pr.ds, pr.K, pr.Kp, e); break;
+    case 3: lambda_body<Eq, 3>(tb.t3, pr.q, pr.U, pr.ds, pr.K, pr.Kp, e); break;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // launchers: dispatch on p to the template instance
 // ---------------------------------------------------------------------------
-inline unsigned nblk(int n) { return (unsigned)((n + kBlock - 1) / kBlock); }
+inline unsigned nblk(int n, int b = kBlock) { return (unsigned)((n + b - 1) / b); }
 
 template <class Eq>
 struct Launch {
@@ -559,41 +766,70 @@ struct Launch {
     case 5: { constexpr int P = 5; expr; } break; \
   }
 
+  static ElemArgs eargs(const Ctx &c, double *us, const double *un, double *out, double ca,
+                        double cb, double cc, const double *dtp, double *T, int check) {
+    ElemArgs a;
+    a.us = us;
+    a.un = un;
+    a.out = out;
+    a.Fh = c.Fh;
+    a.esd = c.m.esd;
+    a.geo = c.m.geo;
+    a.dtp = dtp;
+    a.bathy = c.m.bathy;
+    a.T = T;
+    a.ca = ca;
+    a.cb = cb;
+    a.cc = cc;
+    a.K = c.m.K;
+    a.Kp = c.m.Kp;
+    a.check = check;
+    return a;
+  }
+
   static void trace(const Ctx &c, double *u) {
     if (!c.m.K) return;
-    DG_DISPATCH_P((k_trace<Eq, P><<<nblk(c.m.K), kBlock, 0, c.st>>>(tab<P>(c), *c.q, u, c.T,
-                                                                     c.m.K, c.m.Kp)));
+    DG_DISPATCH_P((k_trace<Eq, P><<<nblk(c.m.K, c.blk), c.blk, 0, c.st>>>(tab<P>(c), *c.q, u,
+                                                                          c.T, c.m.K, c.m.Kp)));
   }
   static void face(const Ctx &c, const double *t, double tcoef) {
     if (!c.m.S) return;
-    DG_DISPATCH_P((k_face<Eq, P><<<nblk(c.m.S), kBlock, 0, c.st>>>(
-        tab<P>(c), *c.q, c.T, c.m.side, c.m.sgeo, c.m.bxy, c.Fh, t, &c.ds->dt, tcoef, c.m.S,
-        c.m.Sb)));
+    FaceArgs a;
+    a.T = c.T;
+    a.side = c.m.side;
+    a.sgeo = c.m.sgeo;
+    a.bxy = c.m.bxy;
+    a.Fh = c.Fh;
+    a.tptr = t;
+    a.dtp = &c.ds->dt;
+    a.tcoef = tcoef;
+    a.S = c.m.S;
+    a.Sb = c.m.Sb;
+    DG_DISPATCH_P((k_face<Eq, P><<<nblk(c.m.S, c.blk), c.blk, 0, c.st>>>(tab<P>(c), *c.q, a)));
   }
   static void element(const Ctx &c, double *us, const double *un, double *out, double ca,
                       double cb, double cc, const double *dtp) {
     if (!c.m.K) return;
-    DG_DISPATCH_P((k_element<Eq, P, false><<<nblk(c.m.K), kBlock, 0, c.st>>>(
-        tab<P>(c), *c.q, us, un, out, c.Fh, c.m.esd, c.m.geo, dtp, ca, cb, cc, c.m.K,
-        c.m.Kp, nullptr, 0)));
+    const ElemArgs a = eargs(c, us, un, out, ca, cb, cc, dtp, nullptr, 0);
+    DG_DISPATCH_P((k_element<Eq, P, false><<<nblk(c.m.K, c.blk), c.blk, 0, c.st>>>(tab<P>(c),
+                                                                                   *c.q, a)));
   }
   static void element_tr(const Ctx &c, double *us, const double *un, double *out, double ca,
                          double cb, double cc, const double *dtp, int check) {
     if (!c.m.K) return;
-    DG_DISPATCH_P((k_element<Eq, P, true><<<nblk(c.m.K), kBlock, 0, c.st>>>(
-        tab<P>(c), *c.q, us, un, out, c.Fh, c.m.esd, c.m.geo, dtp, ca, cb, cc, c.m.K,
-        c.m.Kp, c.T, check)));
+    const ElemArgs a = eargs(c, us, un, out, ca, cb, cc, dtp, c.T, check);
+    DG_DISPATCH_P((k_element<Eq, P, true><<<nblk(c.m.K, c.blk), c.blk, 0, c.st>>>(tab<P>(c),
+                                                                                  *c.q, a)));
   }
   static void limit_tr(const Ctx &c, double *u) {
     if (!c.m.K || c.p < 1) return;
-    DG_DISPATCH_P((k_limit_tr<Eq, P><<<nblk(c.m.K), kBlock, 0, c.st>>>(tab<P>(c), *c.q, u, c.T,
-                                                                        c.m.nbr, c.m.K,
-                                                                        c.m.Kp)));
+    DG_DISPATCH_P((k_limit_tr<Eq, P><<<nblk(c.m.K, c.blk), c.blk, 0, c.st>>>(
+        tab<P>(c), *c.q, u, c.T, c.m.nbr, c.m.K, c.m.Kp)));
   }
   static void limit(const Ctx &c, double *u) {
     if (!c.m.K || c.p < 1) return;
-    DG_DISPATCH_P((k_limit<Eq, P><<<nblk(c.m.K), kBlock, 0, c.st>>>(tab<P>(c), u, c.m.nbr,
-                                                                     c.m.K, c.m.Kp)));
+    DG_DISPATCH_P((k_limit<Eq, P><<<nblk(c.m.K, c.blk), c.blk, 0, c.st>>>(tab<P>(c), u, c.m.nbr,
+                                                                          c.m.K, c.m.Kp)));
   }
   static void lambda(const Ctx &c, const double *u) {
     DG_DISPATCH_P((k_lambda<Eq, P><<<nblk(c.m.K), kBlock, 0, c.st>>>(tab<P>(c), *c.q, u, c.ds,
@@ -618,6 +854,33 @@ struct Launch {
   static const Ops &ops() {
     static const Ops o = {trace, face, element, limit, lambda, init, l2err, element_tr,
                           limit_tr, vertex};
+    return o;
+  }
+
+  // ---- batched launches ----
+  static const BatchTabs &btabs(const BatchLaunch &b) {
+    return *reinterpret_cast<const BatchTabs *>(b.tabs);
+  }
+  static void b_trace(const BatchLaunch &b) {
+    k_trace_batch<Eq><<<b.neblk, b.blk, 0, b.st>>>(btabs(b), b.probs, b.eblk2prob, b.eblk0);
+  }
+  static void b_face(const BatchLaunch &b, double tcoef) {
+    k_face_batch<Eq><<<b.nsblk, b.blk, 0, b.st>>>(btabs(b), b.probs, b.sblk2prob, b.sblk0,
+                                                   tcoef);
+  }
+  static void b_element(const BatchLaunch &b, int stage) {
+    k_element_batch<Eq><<<b.neblk, b.blk, 0, b.st>>>(btabs(b), b.probs, b.eblk2prob, b.eblk0,
+                                                      stage, b.limiter ? 0 : 1);
+  }
+  static void b_limit_tr(const BatchLaunch &b, int stage) {
+    k_limit_tr_batch<Eq><<<b.neblk, b.blk, 0, b.st>>>(btabs(b), b.probs, b.eblk2prob, b.eblk0,
+                                                       stage);
+  }
+  static void b_lambda(const BatchLaunch &b) {
+    k_lambda_batch<Eq><<<b.nlblk, kBlock, 0, b.st>>>(btabs(b), b.probs, b.lblk2prob, b.lblk0);
+  }
+  static const BatchOps &batch_ops() {
+    static const BatchOps o = {b_trace, b_face, b_element, b_limit_tr, b_lambda};
     return o;
   }
 };

@@ -3,4 +3,5 @@
 
 namespace dg {
 const Ops &ops_advection() { return Launch<Advection>::ops(); }
+const BatchOps &batch_ops_advection() { return Launch<Advection>::batch_ops(); }
 }  // namespace dg

@@ -113,7 +113,7 @@ void launch_rk4_final(cudaStream_t st, int n, double *c, const double *k1, const
 
 // dt = cfl * d_min / lambda_max / (2p + 1) (time_integrator.cu:217), the
 // last step shortened to land on endtime (:226-231)
-__global__ void k_compute_dt(DevScalars *ds, int p) {
+__device__ __forceinline__ void compute_dt_body(DevScalars *ds, int p) {
   double lam = __longlong_as_double((long long)ds->lam_bits);
   double dt = ds->fixed_dt > 0 ? ds->fixed_dt : ds->cfl * ds->dmin / lam / (2. * p + 1.);
   if (!(dt == dt) || !(dt > 0) || isinf(dt)) {
@@ -130,10 +130,48 @@ __global__ void k_compute_dt(DevScalars *ds, int p) {
   }
   ds->dt = dt;
 }
-__global__ void k_reset_lambda(DevScalars *ds) { ds->lam_bits = 0ull; }
-__global__ void k_advance_t(DevScalars *ds) {
+__device__ __forceinline__ void advance_t_body(DevScalars *ds) {
   if (ds->dt > 0) ds->steps++;
   ds->t = ds->last ? ds->endtime : ds->t + ds->dt;
+}
+__global__ void k_compute_dt(DevScalars *ds, int p) { compute_dt_body(ds, p); }
+__global__ void k_reset_lambda(DevScalars *ds) { ds->lam_bits = 0ull; }
+__global__ void k_advance_t(DevScalars *ds) { advance_t_body(ds); }
+
+// one thread per problem of a batch
+__global__ void k_batch_reset_lambda(BatchProb *pr, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) pr[i].ds->lam_bits = 0ull;
+}
+__global__ void k_batch_compute_dt(BatchProb *pr, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) compute_dt_body(pr[i].ds, pr[i].p);
+}
+__global__ void k_batch_advance_t(BatchProb *pr, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) advance_t_body(pr[i].ds);
+}
+void launch_batch_reset_lambda(cudaStream_t st, BatchProb *probs, int n) {
+  if (n) k_batch_reset_lambda<<<grid_for(n), kB, 0, st>>>(probs, n);
+}
+void launch_batch_compute_dt(cudaStream_t st, BatchProb *probs, int n) {
+  if (n) k_batch_compute_dt<<<grid_for(n), kB, 0, st>>>(probs, n);
+}
+void launch_batch_advance_t(cudaStream_t st, BatchProb *probs, int n) {
+  if (n) k_batch_advance_t<<<grid_for(n), kB, 0, st>>>(probs, n);
+}
+
+struct BatchTabsImage {
+  Tab<1> t1;
+  Tab<2> t2;
+  Tab<3> t3;
+};
+size_t batch_tabs_bytes() { return sizeof(BatchTabsImage); }
+void build_batch_tabs(const void *t1, const void *t2, const void *t3, void *dst) {
+  BatchTabsImage *b = static_cast<BatchTabsImage *>(dst);
+  if (t1) std::memcpy(&b->t1, t1, sizeof(Tab<1>));
+  if (t2) std::memcpy(&b->t2, t2, sizeof(Tab<2>));
+  if (t3) std::memcpy(&b->t3, t3, sizeof(Tab<3>));
 }
 
 void launch_compute_dt(cudaStream_t st, DevScalars *ds, int p) { k_compute_dt<<<1, 1, 0, st>>>(ds, p); }

@@ -3,4 +3,5 @@
 
 namespace dg {
 const Ops &ops_euler() { return Launch<Euler>::ops(); }
+const BatchOps &batch_ops_euler() { return Launch<Euler>::batch_ops(); }
 }  // namespace dg

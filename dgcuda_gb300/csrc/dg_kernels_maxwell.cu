@@ -3,4 +3,5 @@
 
 namespace dg {
 const Ops &ops_maxwell() { return Launch<Maxwell>::ops(); }
+const BatchOps &batch_ops_maxwell() { return Launch<Maxwell>::batch_ops(); }
 }  // namespace dg

@@ -3,4 +3,5 @@
 
 namespace dg {
 const Ops &ops_shallow_water() { return Launch<ShallowWater>::ops(); }
+const BatchOps &batch_ops_shallow_water() { return Launch<ShallowWater>::batch_ops(); }
 }  // namespace dg

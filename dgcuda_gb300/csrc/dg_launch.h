@@ -8,7 +8,12 @@
 
 namespace dg {
 
-struct EqP;
+// equation / problem parameters (kernel parameter)
+struct EqP {
+  double gamma, g, ax, ay, mu, eps;
+  int problem, pad;
+  double prm[8];
+};
 
 // Device-resident mesh in internal (space-filling-curve) element order.
 // Per-element arrays are rows of length Kp (K rounded up to 32) so every
@@ -24,6 +29,7 @@ struct DevMesh {
   double *sgeo = nullptr; // 3 rows of S: nx, ny, len / 2
   double *bxy = nullptr;  // 4 rows of Sb: start and end vertex of the left face (boundary sides)
   int *perm = nullptr;    // K: internal index -> caller's (.pmsh) index
+  double *bathy = nullptr; // shallow water bed modes [mode][Kp], null = flat
 };
 
 // device scalars used by graph-captured steps
@@ -46,12 +52,55 @@ struct Ctx {
   cudaStream_t st = nullptr;
   DevMesh m;
   int p = 1, eq = 0, N = 1, np = 3;
+  int blk = 128;                  // block size of the stage kernels (autotuned)
   const EqP *q = nullptr;         // host copy of the equation parameters
   const void *tab = nullptr;      // host Tab<p> image
   double *T = nullptr;            // traces [elem][face][j][var]
   double *Fh = nullptr;           // face fluxes [side][j][var], scaled by len/2 * w_j
   DevScalars *ds = nullptr;       // device scalars
 };
+
+// one problem of a batched ensemble (device resident)
+struct BatchProb {
+  int p, K, Kp, S, Sb, pad;
+  double *U, *W, *T, *Fh;
+  const double *geo;
+  const int *esd, *nbr;
+  const int4 *side;
+  const double *sgeo, *bxy, *bathy;
+  DevScalars *ds;
+  EqP q;
+};
+
+struct BatchLaunch {
+  cudaStream_t st = nullptr;
+  const void *tabs = nullptr;       // BatchTabs image (Tab<1>, Tab<2>, Tab<3>)
+  BatchProb *probs = nullptr;       // device array
+  int nprob = 0, blk = 128, limiter = 0;
+  const int *eblk2prob = nullptr, *eblk0 = nullptr;  // element blocks of size blk
+  const int *sblk2prob = nullptr, *sblk0 = nullptr;  // side blocks of size blk
+  const int *lblk2prob = nullptr, *lblk0 = nullptr;  // element blocks of 128 (wave speed)
+  int neblk = 0, nsblk = 0, nlblk = 0;
+};
+
+struct BatchOps {
+  void (*trace)(const BatchLaunch &);
+  void (*face)(const BatchLaunch &, double tcoef);
+  void (*element)(const BatchLaunch &, int stage);
+  void (*limit_tr)(const BatchLaunch &, int stage);
+  void (*lambda)(const BatchLaunch &);
+};
+
+const BatchOps &batch_ops_advection();
+const BatchOps &batch_ops_euler();
+const BatchOps &batch_ops_shallow_water();
+const BatchOps &batch_ops_maxwell();
+size_t batch_tabs_bytes();
+// copies the Tab<1>, Tab<2>, Tab<3> images into a BatchTabs image
+void build_batch_tabs(const void *t1, const void *t2, const void *t3, void *dst);
+void launch_batch_reset_lambda(cudaStream_t st, BatchProb *probs, int n);
+void launch_batch_compute_dt(cudaStream_t st, BatchProb *probs, int n);
+void launch_batch_advance_t(cudaStream_t st, BatchProb *probs, int n);
 
 struct Ops {
   // edge traces of u; flattens (in u) any element with a non-physical trace

@@ -45,6 +45,8 @@ struct dg_solver {
   const dg::Ops *ops = nullptr;
   double *U = nullptr, *W = nullptr, *k[4] = {nullptr, nullptr, nullptr, nullptr};
   double *ubuf = nullptr, *partial = nullptr, *T = nullptr, *Fh = nullptr, *vbuf = nullptr;
+  double *bathy = nullptr;        // bed modes (shallow water), internal order
+  std::vector<double> mesh_v;     // vertices per element, .pmsh order (bed projection)
   dg::DevScalars *ds = nullptr;
   double dmin = 0;
   size_t ndof_p = 0;  // N * np * Kp
@@ -459,6 +461,9 @@ extern "C" dg_status dg_solver_create(const dg_mesh *mesh, dg_equation eq, int p
     }
   }
   s->dmin = dmin;
+  s->mesh_v.resize((size_t)6 * K);
+  for (int o = 0; o < K; o++)
+    for (int k = 0; k < 6; k++) s->mesh_v[(size_t)6 * o + k] = mesh->V[k][o];
   // ---- side arrays ----
   std::vector<int4> side(S);
   std::vector<double> sgeo((size_t)3 * S), bxy((size_t)4 * std::max(Sb, 1));
@@ -736,6 +741,386 @@ extern "C" dg_status dg_l2_error(dg_solver *s, double t, double *err) {
     err[n] = std::sqrt(a);
   }
   return DG_OK;
+}
+
+// ---- shallow-water bed ---------------------------------------------------
+extern "C" dg_status dg_set_bathymetry(dg_solver *s, const double *b) {
+  if (!s) return fail(DG_BAD_ARG, "null solver");
+  if (s->eq != DG_SHALLOW_WATER) return fail(DG_UNSUPPORTED, "bathymetry needs shallow water");
+  CK(cudaSetDevice(s->device));
+  if (!b) {
+    s->m.bathy = nullptr;
+  } else {
+    if (!s->bathy) {
+      dg_status st = dalloc(s, &s->bathy, (size_t)s->np * s->m.Kp);
+      if (st != DG_OK) return st;
+    }
+    CK(cudaMemcpyAsync(s->ubuf, b, (size_t)s->np * s->K * sizeof(double),
+                       cudaMemcpyHostToDevice, s->st));
+    dg::launch_permute_in(s->st, s->ubuf, s->bathy, s->m.perm, s->np, s->K, s->m.Kp);
+    s->m.bathy = s->bathy;
+  }
+  s->ctx.m.bathy = s->m.bathy;
+  drop_graphs(s);
+  return sync_check(s);
+}
+
+extern "C" dg_status dg_get_bathymetry(dg_solver *s, double *b) {
+  if (!s || !b) return fail(DG_BAD_ARG, "null argument");
+  if (!s->m.bathy) {
+    std::memset(b, 0, sizeof(double) * (size_t)s->np * s->K);
+    return DG_OK;
+  }
+  CK(cudaSetDevice(s->device));
+  dg::launch_permute_out(s->st, s->m.bathy, s->ubuf, s->m.perm, s->np, s->K, s->m.Kp);
+  CK(cudaMemcpyAsync(b, s->ubuf, (size_t)s->np * s->K * sizeof(double), cudaMemcpyDeviceToHost,
+                     s->st));
+  return sync_check(s);
+}
+
+extern "C" dg_status dg_bathymetry_project(dg_solver *s, int kind, const double *prm) {
+  if (!s) return fail(DG_BAD_ARG, "null solver");
+  if (kind == DG_BED_FLAT) return dg_set_bathymetry(s, nullptr);
+  if (!prm) return fail(DG_BAD_ARG, "null parameters");
+  if (kind != DG_BED_SINE && kind != DG_BED_LINEAR) return fail(DG_BAD_ARG, "unknown bed kind");
+  // b_i = sum_q w_q b(x_q) phi_i(q) per element (orthonormal basis, as evalU0)
+  const dg_order_tables &T = s->tables;
+  std::vector<double> b((size_t)s->np * s->K);
+  for (int e = 0; e < s->K; e++) {
+    const double *V = s->mesh_v.data() + (size_t)6 * e;
+    for (int i = 0; i < s->np; i++) {
+      double acc = 0;
+      for (int q = 0; q < T.n_q; q++) {
+        double r = T.r[q], ss = T.s[q];
+        double x = V[2] * r + V[4] * ss + V[0] * (1 - r - ss);
+        double y = V[3] * r + V[5] * ss + V[1] * (1 - r - ss);
+        double bv = kind == DG_BED_SINE
+                        ? prm[0] * std::sin(2 * dg::kPi * prm[1] * x) * std::sin(2 * dg::kPi * prm[2] * y)
+                        : prm[0] + prm[1] * x + prm[2] * y;
+        acc += T.w[q] * bv * T.B[q][i];
+      }
+      b[(size_t)i * s->K + e] = acc;
+    }
+  }
+  return dg_set_bathymetry(s, b.data());
+}
+
+// ---- block-size autotuner --------------------------------------------------
+namespace {
+template <class F>
+dg_status time_steps(cudaStream_t st, F &&step, float *ms) {
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  cudaEventRecord(a, st);
+  dg_status r = step();
+  cudaEventRecord(b, st);
+  cudaEventSynchronize(b);
+  cudaEventElapsedTime(ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return r;
+}
+const int kTuneBlocks[] = {64, 128, 256};
+}  // namespace
+
+extern "C" dg_status dg_autotune(dg_solver *s, int *block) {
+  if (!s) return fail(DG_BAD_ARG, "null solver");
+  CK(cudaSetDevice(s->device));
+  double *save = nullptr;
+  CK(cudaMalloc(&save, s->ndof_p * sizeof(double)));
+  CK(cudaMemcpyAsync(save, s->U, s->ndof_p * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
+  int best = s->ctx.blk;
+  float best_ms = 1e30f;
+  for (int blk : kTuneBlocks) {
+    s->ctx.blk = blk;
+    drop_graphs(s);
+    double t = 0;
+    dg_status st = run_steps(s, 1, DG_SSP_RK3, 0.0, 0.0, &t, nullptr);  // capture + warm
+    float ms = 0;
+    if (st == DG_OK)
+      st = time_steps(s->st, [&] { return run_steps(s, 3, DG_SSP_RK3, 0.0, 0.0, &t, nullptr); },
+                      &ms);
+    cudaMemcpyAsync(s->U, save, s->ndof_p * sizeof(double), cudaMemcpyDeviceToDevice, s->st);
+    if (st != DG_OK) {
+      cudaFree(save);
+      return st;
+    }
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = blk;
+    }
+  }
+  cudaStreamSynchronize(s->st);
+  cudaFree(save);
+  s->ctx.blk = best;
+  drop_graphs(s);
+  if (block) *block = best;
+  return DG_OK;
+}
+
+// ---- batched ensembles -------------------------------------------------------
+struct dg_batch {
+  std::vector<dg_solver *> m;
+  int device = 0, blk = 128, limiter = 0;
+  dg_equation eq = DG_SHALLOW_WATER;
+  cudaStream_t st = nullptr;
+  const dg::BatchOps *ops = nullptr;
+  std::vector<char> tabs;
+  dg::BatchProb *probs = nullptr;
+  int *maps = nullptr;  // device: element/side/lambda block maps
+  dg::BatchLaunch bl;
+  cudaGraphExec_t graph = nullptr;
+  long long graph_nodes = 0, launches = 0;
+};
+
+namespace {
+const dg::BatchOps *batch_ops_for(dg_equation eq) {
+  switch (eq) {
+    case DG_ADVECTION: return &dg::batch_ops_advection();
+    case DG_EULER: return &dg::batch_ops_euler();
+    case DG_SHALLOW_WATER: return &dg::batch_ops_shallow_water();
+    case DG_MAXWELL: return &dg::batch_ops_maxwell();
+  }
+  return nullptr;
+}
+
+// block -> problem maps for blocks of `blk` elements (or sides)
+void block_maps(const std::vector<int> &count, int blk, std::vector<int> &b2p,
+                std::vector<int> &b0) {
+  b2p.clear();
+  b0.assign(count.size(), 0);
+  for (size_t i = 0; i < count.size(); i++) {
+    b0[i] = (int)b2p.size();
+    int nb = (count[i] + blk - 1) / blk;
+    for (int k = 0; k < nb; k++) b2p.push_back((int)i);
+  }
+}
+
+dg_status batch_build_maps(dg_batch *b) {
+  std::vector<int> ke, ks;
+  for (auto *s : b->m) {
+    ke.push_back(s->K);
+    ks.push_back(s->S);
+  }
+  std::vector<int> e2p, e0, s2p, s0, l2p, l0;
+  block_maps(ke, b->blk, e2p, e0);
+  block_maps(ks, b->blk, s2p, s0);
+  block_maps(ke, 128, l2p, l0);
+  std::vector<int> all;
+  size_t oe2p = 0, oe0 = oe2p + e2p.size(), os2p = oe0 + e0.size(), os0 = os2p + s2p.size(),
+         ol2p = os0 + s0.size(), ol0 = ol2p + l2p.size();
+  for (auto *v : {&e2p, &e0, &s2p, &s0, &l2p, &l0}) all.insert(all.end(), v->begin(), v->end());
+  if (b->maps) cudaFree(b->maps);
+  b->maps = nullptr;
+  CK(cudaMalloc(&b->maps, all.size() * sizeof(int)));
+  CK(cudaMemcpy(b->maps, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice));
+  dg::BatchLaunch &L = b->bl;
+  L.eblk2prob = b->maps + oe2p;
+  L.eblk0 = b->maps + oe0;
+  L.sblk2prob = b->maps + os2p;
+  L.sblk0 = b->maps + os0;
+  L.lblk2prob = b->maps + ol2p;
+  L.lblk0 = b->maps + ol0;
+  L.neblk = (int)e2p.size();
+  L.nsblk = (int)s2p.size();
+  L.nlblk = (int)l2p.size();
+  L.blk = b->blk;
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  b->graph = nullptr;
+  return DG_OK;
+}
+
+// one SSP-RK3 step of every member (launch sequence, capturable)
+void batch_step_seq(dg_batch *b) {
+  const dg::BatchLaunch &L = b->bl;
+  dg::launch_batch_reset_lambda(L.st, L.probs, L.nprob);
+  b->ops->lambda(L);
+  dg::launch_batch_compute_dt(L.st, L.probs, L.nprob);
+  const double tc[3] = {0.0, 1.0, 0.5};
+  for (int stage = 0; stage < 3; stage++) {
+    b->ops->face(L, tc[stage]);
+    b->ops->element(L, stage);
+    if (L.limiter) b->ops->limit_tr(L, stage);
+  }
+  dg::launch_batch_advance_t(L.st, L.probs, L.nprob);
+}
+
+dg_status batch_run(dg_batch *b, int nsteps, double *t) {
+  CK(cudaSetDevice(b->device));
+  for (size_t i = 0; i < b->m.size(); i++) {
+    dg_solver *s = b->m[i];
+    CK(cudaStreamSynchronize(s->st));
+    dg::DevScalars h{};
+    h.t = t ? t[i] : 0.0;
+    h.one = 1.0;
+    h.dmin = s->dmin;
+    h.cfl = s->prm.cfl;
+    CK(cudaMemcpyAsync(s->ds, &h, sizeof h, cudaMemcpyHostToDevice, b->st));
+    // the reference limits once before its step loop (time_integrator.cu:178-184)
+    if (b->limiter && s->np >= 3) {
+      dg::Ctx c = s->ctx;
+      c.st = b->st;
+      s->ops->limit(c, s->U);
+      b->launches++;
+    }
+  }
+  b->ops->trace(b->bl);
+  b->launches++;
+  if (!b->graph) {
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+    batch_step_seq(b);
+    cudaError_t e = cudaStreamEndCapture(b->st, &g);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    size_t nn = 0;
+    cudaGraphGetNodes(g, nullptr, &nn);
+    b->graph_nodes = (long long)nn;
+    e = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+  }
+  for (int k = 0; k < nsteps; k++) {
+    CK(cudaGraphLaunch(b->graph, b->st));
+    b->launches += b->graph_nodes;
+  }
+  cudaError_t e = cudaStreamSynchronize(b->st);
+  if (e != cudaSuccess) return cuda_fail(e, "batched step");
+  int nan = 0;
+  for (size_t i = 0; i < b->m.size(); i++) {
+    dg::DevScalars h{};
+    CK(cudaMemcpy(&h, b->m[i]->ds, sizeof h, cudaMemcpyDeviceToHost));
+    if (t) t[i] = h.t;
+    if (h.status == 4) nan = 1;
+  }
+  if (nan) return fail(DG_NAN, "a batch member's time step is NaN or not positive");
+  return DG_OK;
+}
+}  // namespace
+
+extern "C" dg_status dg_batch_create(int n, dg_solver *const *members, dg_batch **out) {
+  if (!out || !members || n <= 0) return fail(DG_BAD_ARG, "bad batch arguments");
+  *out = nullptr;
+  dg_batch *b = new dg_batch();
+  auto bail = [&](dg_status st) {
+    dg_batch_destroy(b);
+    return st;
+  };
+  const void *timg[4] = {nullptr, nullptr, nullptr, nullptr};
+  for (int i = 0; i < n; i++) {
+    dg_solver *s = members[i];
+    if (!s) return bail(fail(DG_BAD_ARG, "null batch member"));
+    if (i == 0) {
+      b->device = s->device;
+      b->eq = s->eq;
+      b->limiter = s->prm.limiter ? 1 : 0;
+    }
+    if (s->device != b->device || s->eq != b->eq)
+      return bail(fail(DG_BAD_ARG, "batch members must share device and equation"));
+    if ((s->prm.limiter ? 1 : 0) != b->limiter)
+      return bail(fail(DG_BAD_ARG, "batch members must agree on the limiter"));
+    if (s->p < 1 || s->p > 3) return bail(fail(DG_UNSUPPORTED, "batched orders are p = 1..3"));
+    if (!timg[s->p]) timg[s->p] = s->tabimg.data();
+    b->m.push_back(s);
+  }
+  if (cudaSetDevice(b->device) != cudaSuccess) return bail(fail(DG_CUDA_ERROR, "cudaSetDevice"));
+  if (cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(fail(DG_CUDA_ERROR, "cudaStreamCreate"));
+  b->ops = batch_ops_for(b->eq);
+  b->tabs.resize(dg::batch_tabs_bytes());
+  dg::build_batch_tabs(timg[1], timg[2], timg[3], b->tabs.data());
+  std::vector<dg::BatchProb> hp(n);
+  for (int i = 0; i < n; i++) {
+    dg_solver *s = b->m[i];
+    dg::BatchProb &q = hp[i];
+    std::memset(&q, 0, sizeof q);
+    q.p = s->p;
+    q.K = s->K;
+    q.Kp = s->m.Kp;
+    q.S = s->S;
+    q.Sb = s->m.Sb;
+    q.U = s->U;
+    q.W = s->W;
+    q.T = s->T;
+    q.Fh = s->Fh;
+    q.geo = s->m.geo;
+    q.esd = s->m.esd;
+    q.nbr = s->m.nbr;
+    q.side = s->m.side;
+    q.sgeo = s->m.sgeo;
+    q.bxy = s->m.bxy;
+    q.bathy = s->m.bathy;
+    q.ds = s->ds;
+    q.q = s->q;
+  }
+  if (cudaMalloc(&b->probs, sizeof(dg::BatchProb) * n) != cudaSuccess)
+    return bail(fail(DG_CUDA_ERROR, "cudaMalloc"));
+  if (cudaMemcpy(b->probs, hp.data(), sizeof(dg::BatchProb) * n, cudaMemcpyHostToDevice) !=
+      cudaSuccess)
+    return bail(fail(DG_CUDA_ERROR, "cudaMemcpy"));
+  b->bl.st = b->st;
+  b->bl.tabs = b->tabs.data();
+  b->bl.probs = b->probs;
+  b->bl.nprob = n;
+  b->bl.limiter = b->limiter;
+  dg_status st = batch_build_maps(b);
+  if (st != DG_OK) return bail(st);
+  *out = b;
+  return DG_OK;
+}
+
+extern "C" dg_status dg_batch_step(dg_batch *b, int nsteps, double *t) {
+  if (!b || nsteps < 0) return fail(DG_BAD_ARG, "bad batch step arguments");
+  return batch_run(b, nsteps, t);
+}
+
+extern "C" dg_status dg_batch_autotune(dg_batch *b, int *block) {
+  if (!b) return fail(DG_BAD_ARG, "null batch");
+  CK(cudaSetDevice(b->device));
+  std::vector<double *> save(b->m.size(), nullptr);
+  for (size_t i = 0; i < b->m.size(); i++) {
+    CK(cudaMalloc(&save[i], b->m[i]->ndof_p * sizeof(double)));
+    CK(cudaMemcpy(save[i], b->m[i]->U, b->m[i]->ndof_p * sizeof(double),
+                  cudaMemcpyDeviceToDevice));
+  }
+  int best = b->blk;
+  float best_ms = 1e30f;
+  std::vector<double> t(b->m.size(), 0.0);
+  dg_status st = DG_OK;
+  for (int blk : kTuneBlocks) {
+    b->blk = blk;
+    if ((st = batch_build_maps(b)) != DG_OK) break;
+    if ((st = batch_run(b, 1, t.data())) != DG_OK) break;
+    float ms = 0;
+    st = time_steps(b->st, [&] { return batch_run(b, 3, t.data()); }, &ms);
+    for (size_t i = 0; i < b->m.size(); i++)
+      cudaMemcpy(b->m[i]->U, save[i], b->m[i]->ndof_p * sizeof(double),
+                 cudaMemcpyDeviceToDevice);
+    if (st != DG_OK) break;
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = blk;
+    }
+  }
+  for (auto *p : save) cudaFree(p);
+  if (st != DG_OK) return st;
+  b->blk = best;
+  st = batch_build_maps(b);
+  if (block) *block = best;
+  return st;
+}
+
+extern "C" long long dg_batch_launches(const dg_batch *b) { return b ? b->launches : 0; }
+
+extern "C" void dg_batch_destroy(dg_batch *b) {
+  if (!b) return;
+  cudaSetDevice(b->device);
+  if (b->st) cudaStreamSynchronize(b->st);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  if (b->maps) cudaFree(b->maps);
+  if (b->probs) cudaFree(b->probs);
+  if (b->st) cudaStreamDestroy(b->st);
+  delete b;
 }
 
 extern "C" dg_status dg_eval_vertices(dg_solver *s, int var, double *uv) {

@@ -166,6 +166,40 @@ dg_status dg_l2_error(dg_solver *s, double t, double *err);
  * (conserv_kernels.cu:1284-1307, main.cu:69-116) */
 dg_status dg_eval_vertices(dg_solver *s, int var, double *uv);
 
+/* ---- shallow-water bed (the reference's source_term hook,
+ * conserv_kernels.cu:1063; its modules define no bed) -----------------------
+ * source (0, -g h b_x, -g h b_y) with b a DG field of the solver's order:
+ * b = modes [mode][elem] (.pmsh order, n_p x K), or NULL for a flat bed */
+dg_status dg_set_bathymetry(dg_solver *s, const double *b);
+/* the bed modes in the same layout (zeros for a flat bed) */
+dg_status dg_get_bathymetry(dg_solver *s, double *b);
+#define DG_BED_FLAT 0
+#define DG_BED_SINE 1   /* b = prm[0] sin(2 pi prm[1] x) sin(2 pi prm[2] y) */
+#define DG_BED_LINEAR 2 /* b = prm[0] + prm[1] x + prm[2] y */
+/* L2 projection of an analytic bed onto the basis, then dg_set_bathymetry */
+dg_status dg_bathymetry_project(dg_solver *s, int kind, const double *prm);
+
+/* Block size (elements per block, one thread per element) of the stage
+ * kernels, chosen by timing SSP-RK3 steps with 64, 128 and 256; the state is
+ * restored afterwards.  *block receives the choice. */
+dg_status dg_autotune(dg_solver *s, int *block);
+
+/* ---- batched ensembles: independent problems stepped together -----------
+ * One launch per kernel per RK stage covers every member (concatenated
+ * element ranges; each member keeps its own mesh, order p in 1..3, CFL time
+ * step and time), and one SSP-RK3 step of the whole ensemble is one CUDA
+ * graph.  Members must share device, equation and limiter setting; they
+ * stay owned by the caller and must outlive the batch.  No reference
+ * counterpart (DGCUDA runs one problem per process). */
+typedef struct dg_batch dg_batch;
+dg_status dg_batch_create(int n, dg_solver *const *members, dg_batch **out);
+/* nsteps SSP-RK3 steps of every member; t[i] is member i's time (read and
+ * advanced) */
+dg_status dg_batch_step(dg_batch *b, int nsteps, double *t);
+dg_status dg_batch_autotune(dg_batch *b, int *block);
+long long dg_batch_launches(const dg_batch *b);
+void dg_batch_destroy(dg_batch *b);
+
 /* Timing of the solver's own kernels (CUDA events around each launch on the
  * solver stream).  When enabled, dg_step launches kernels directly instead
  * of replaying a CUDA graph. */

@@ -75,6 +75,7 @@ typedef struct or_solver {
   /* work */
   double *vol, *sl, *sr;
   int flattened;
+  double *bathy; /* shallow-water bed modes [mode][elem] or NULL (extension) */
 } or_solver;
 
 static double dmin2(double a, double b) { return a < b ? a : b; }
@@ -492,8 +493,21 @@ or_solver *or_create(int eq, int p, int K, int S, const double *V, const int *es
   return o;
 }
 
+/* shallow-water bed modes [mode][elem] (copied), or NULL for a flat bed */
+int or_set_bathymetry(or_solver *o, const double *b) {
+  free(o->bathy);
+  o->bathy = 0;
+  if (b) {
+    size_t n = (size_t)o->np * o->K;
+    o->bathy = (double *)xmalloc(sizeof(double) * n);
+    memcpy(o->bathy, b, sizeof(double) * n);
+  }
+  return 0;
+}
+
 void or_destroy(or_solver *o) {
   if (!o) return;
+  free(o->bathy);
   free(o->V);
   free(o->es);
   free(o->sxy);
@@ -642,7 +656,22 @@ static void dg_operator(or_solver *o, double *C, double t, double dt, double *ou
         for (int n = 0; n < N; n++)
           acc[n * NPM + i] += fx[n] * (o->GR[q][i] * ys - o->GS[q][i] * yr) +
                               fy[n] * (-o->GR[q][i] * xs + o->GS[q][i] * xr);
-      /* source term: zero for every module here (euler.cu:282-287) */
+      /* source term (euler.cu:282-287 defines it zero); extension: the
+       * shallow-water bed slope -g h grad b, with w_q J grad b from the
+       * weighted gradient tables, projected on phi_i */
+      if (o->bathy && o->eq == EQ_SW) {
+        double br = 0, bs = 0;
+        for (int i = 1; i < np; i++) {
+          br += o->bathy[(size_t)i * K + e] * o->GR[q][i];
+          bs += o->bathy[(size_t)i * K + e] * o->GS[q][i];
+        }
+        double gh = -o->g * U[0];
+        double sx = gh * (ys * br - yr * bs), sy = gh * (xr * bs - xs * br);
+        for (int i = 0; i < np; i++) {
+          acc[1 * NPM + i] += sx * o->B[q][i];
+          acc[2 * NPM + i] += sy * o->B[q][i];
+        }
+      }
     }
     for (int n = 0; n < N; n++)
       for (int i = 0; i < np; i++) vol[CI(n, i, e)] = acc[n * NPM + i];

@@ -60,6 +60,7 @@ def lib():
         L.or_flattened.argtypes = [C.c_void_p]
         L.or_set_threads.argtypes = [C.c_int]
         L.or_get_tables.argtypes = [C.c_void_p, _dp]
+        L.or_set_bathymetry.argtypes = [C.c_void_p, _dp]
         _L = L
     return _L
 
@@ -113,6 +114,14 @@ class Oracle:
         rc = self.L.or_set_tables(self.h, nq, n1, *[_d(a) for a in parts])
         if rc:
             raise ValueError("table size mismatch")
+
+    def set_bathymetry(self, b):
+        """Bed modes [mode][elem] (shallow water), or None for flat."""
+        if b is None:
+            self.L.or_set_bathymetry(self.h, None)
+        else:
+            self._bathy = np.ascontiguousarray(b, dtype=np.float64).reshape(self.np, self.K)
+            self.L.or_set_bathymetry(self.h, _d(self._bathy))
 
     def tables(self):
         """The oracle's tabulation in the reference's flat layout."""
