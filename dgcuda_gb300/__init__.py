@@ -8,7 +8,7 @@ back as DGError (the reference calls exit()).  All numerics run in the native
 library; there is no Python fallback -- importing fails loudly when
 libdg_gb300.so is missing.
 """
-from .api import (DGError, Mesh, Solver, Batch, Params, lib_path, load_library,  # noqa: F401
+from .api import (DGError, Mesh, Solver, Batch, Adjoint, Params, lib_path, load_library,  # noqa: F401
                   ADVECTION, EULER, SHALLOW_WATER, MAXWELL, SSP_RK3, RK4, RK2,
                   BC_REFLECT, BC_OUTFLOW, BC_INFLOW, BC_TRANSMISSIVE, PERIODIC, PROBLEMS,
                   n_modes, n_vars, measure_fp64_peak)

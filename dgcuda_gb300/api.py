@@ -111,6 +111,14 @@ def _declare(L):
         "dg_batch_autotune": (C.c_int, [C.c_void_p, _ip]),
         "dg_batch_launches": (C.c_longlong, [C.c_void_p]),
         "dg_batch_destroy": (None, [C.c_void_p]),
+        "dg_rhs_tl": (C.c_int, [C.c_void_p, C.c_double, _dp, _dp, _dp, _dp]),
+        "dg_rhs_adjoint": (C.c_int, [C.c_void_p, C.c_double, _dp, _dp, _dp, _dp]),
+        "dg_adjoint_create": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, C.POINTER(C.c_void_p)]),
+        "dg_adjoint_forward": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_int, C.c_int,
+                                         C.c_double, _dp]),
+        "dg_adjoint_backward": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
+        "dg_adjoint_tangent": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
+        "dg_adjoint_destroy": (None, [C.c_void_p]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(L, name, None)
@@ -149,6 +157,54 @@ class Batch:
         h = getattr(self, "_h", None)
         if h is not None and h.value:
             self._L.dg_batch_destroy(h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+class Adjoint:
+    """Discrete adjoint of the shallow-water SSP-RK3 model (dg_adjoint):
+    samples of h at receivers, checkpointed reverse sweep."""
+
+    def __init__(self, solver, rx, ry):
+        self._L = load_library()
+        self.solver = solver
+        rx = np.ascontiguousarray(rx, dtype=np.float64)
+        ry = np.ascontiguousarray(ry, dtype=np.float64)
+        self.nrec = len(rx)
+        h = C.c_void_p()
+        _check(self._L.dg_adjoint_create(solver._h, self.nrec, _dptr(rx), _dptr(ry), C.byref(h)))
+        self._h = h
+        self.nsamp = 0
+
+    def forward(self, nsteps, dt, every, ckpt=50, t0=0.0):
+        self.nsamp = nsteps // every
+        out = np.empty((max(self.nsamp, 1), max(self.nrec, 1)))
+        _check(self._L.dg_adjoint_forward(self._h, nsteps, dt, every, ckpt, t0, _dptr(out)))
+        return out[:self.nsamp, :self.nrec]
+
+    def backward(self, sbar):
+        s = self.solver
+        sbar = np.ascontiguousarray(sbar, dtype=np.float64).reshape(self.nsamp, self.nrec)
+        gu = np.empty(s.shape)
+        gb = np.empty((s.n_p, s.K))
+        _check(self._L.dg_adjoint_backward(self._h, _dptr(sbar), _dptr(gu), _dptr(gb)))
+        return gu, gb
+
+    def tangent(self, du0=None, db=None):
+        s = self.solver
+        out = np.empty((max(self.nsamp, 1), max(self.nrec, 1)))
+        a = None if du0 is None else np.ascontiguousarray(du0, dtype=np.float64).reshape(s.shape)
+        b = None if db is None else np.ascontiguousarray(db, dtype=np.float64).reshape(s.n_p, s.K)
+        _check(self._L.dg_adjoint_tangent(self._h, None if a is None else _dptr(a),
+                                          None if b is None else _dptr(b), _dptr(out)))
+        return out[:self.nsamp, :self.nrec]
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._L.dg_adjoint_destroy(h)
             self._h = None
 
     def __del__(self):
@@ -359,6 +415,27 @@ class Solver:
         b = C.c_int()
         _check(self._L.dg_autotune(self._h, C.byref(b)))
         return b.value
+
+    def rhs_tl(self, c, dc, db=None, t=0.0):
+        """Tangent-linear right-hand side (shallow water)."""
+        c = np.ascontiguousarray(c, dtype=np.float64).reshape(self.shape)
+        dc = np.ascontiguousarray(dc, dtype=np.float64).reshape(self.shape)
+        out = np.empty(self.shape)
+        dbp = None
+        if db is not None:
+            db = np.ascontiguousarray(db, dtype=np.float64).reshape(self.n_p, self.K)
+            dbp = _dptr(db)
+        _check(self._L.dg_rhs_tl(self._h, t, _dptr(c), _dptr(dc), dbp, _dptr(out)))
+        return out
+
+    def rhs_adjoint(self, c, lbar, t=0.0):
+        """(dL/du)^T lbar and (dL/db)^T lbar (shallow water)."""
+        c = np.ascontiguousarray(c, dtype=np.float64).reshape(self.shape)
+        lbar = np.ascontiguousarray(lbar, dtype=np.float64).reshape(self.shape)
+        cb = np.empty(self.shape)
+        bb = np.empty((self.n_p, self.K))
+        _check(self._L.dg_rhs_adjoint(self._h, t, _dptr(c), _dptr(lbar), _dptr(cb), _dptr(bb)))
+        return cb, bb
 
     def stream(self):
         return self._L.dg_solver_stream(self._h)

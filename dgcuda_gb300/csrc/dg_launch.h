@@ -153,6 +153,22 @@ void launch_compute_dt(cudaStream_t st, DevScalars *ds, int p);
 void launch_reset_lambda(cudaStream_t st, DevScalars *ds);
 void launch_advance_t(cudaStream_t st, DevScalars *ds);
 
+// ---- shallow-water tangent-linear / adjoint operators (dg_adjoint.cu) ----
+// (c.T must hold the traces of the linearisation state us; c.Fh carries the
+// tangent fluxes between tl_face and tl_element)
+bool lin_supported(int p);
+bool lin_trace(const Ctx &c, const double *u, const double *scale, double sc, double *Tv);
+bool tl_face(const Ctx &c, const double *Tv, double *dFh);
+bool adj_face(const Ctx &c, const double *Tbar, double *UbL, double *UbR);
+bool tl_element(const Ctx &c, const double *us, const double *dus, const double *db,
+                const double *dun, double *dout, double ca, double cb, double ccdt);
+bool adj_element(const Ctx &c, const double *us, const double *obar, double *ubar_s,
+                 double *bbar, const double *UbL, const double *UbR, double cb, double ccdt);
+void launch_sample(cudaStream_t st, const double *u, const int *el, const double *phi, int nrec,
+                   int np, int Kp, double *out);
+void launch_sample_adj(cudaStream_t st, double *ubar, const int *el, const double *phi, int nrec,
+                       int np, int Kp, const double *sbar);
+
 // what other files need to launch a solver's kernels
 struct SolverView {
   int device = 0;

@@ -46,6 +46,8 @@ struct dg_solver {
   double *U = nullptr, *W = nullptr, *k[4] = {nullptr, nullptr, nullptr, nullptr};
   double *ubuf = nullptr, *partial = nullptr, *T = nullptr, *Fh = nullptr, *vbuf = nullptr;
   double *bathy = nullptr;        // bed modes (shallow water), internal order
+  double *lin_tv = nullptr, *lin_f0 = nullptr, *lin_f1 = nullptr;  // adjoint work
+  bool has_inout_bc = false;      // a side with an inflow or outflow code
   std::vector<double> mesh_v;     // vertices per element, .pmsh order (bed projection)
   dg::DevScalars *ds = nullptr;
   double dmin = 0;
@@ -427,6 +429,10 @@ extern "C" dg_status dg_solver_create(const dg_mesh *mesh, dg_equation eq, int p
   for (int i = 0; i < S; i++) snew[sorder[i]] = i;
   int Sb = 0;
   while (Sb < S && mesh->right[sorder[Sb]] < 0) Sb++;
+  for (int i = 0; i < Sb; i++) {
+    int code = mesh->right[sorder[i]];
+    if (code == DG_BC_INFLOW || code == DG_BC_OUTFLOW) s->has_inout_bc = true;
+  }
 
   // ---- element arrays ----
   std::vector<double> geo((size_t)5 * Kp, 0.0), vtx((size_t)6 * Kp, 0.0), jac(Kp, 1.0);
@@ -1121,6 +1127,437 @@ extern "C" void dg_batch_destroy(dg_batch *b) {
   if (b->probs) cudaFree(b->probs);
   if (b->st) cudaStreamDestroy(b->st);
   delete b;
+}
+
+// ---- tangent-linear and adjoint of the shallow-water step ----------------
+namespace {
+
+struct LinBufs {
+  double *Tv = nullptr, *F0 = nullptr, *F1 = nullptr;
+};
+
+dg_status lin_bufs(dg_solver *s, LinBufs *b) {
+  static_assert(sizeof(LinBufs) > 0, "");
+  const size_t nt = (size_t)s->K * 3 * (s->p + 1) * s->N, nf = (size_t)s->S * (s->p + 1) * s->N;
+  if (!s->lin_tv) {
+    dg_status st;
+    if ((st = dalloc(s, &s->lin_tv, nt)) != DG_OK) return st;
+    if ((st = dalloc(s, &s->lin_f0, nf)) != DG_OK) return st;
+    if ((st = dalloc(s, &s->lin_f1, nf)) != DG_OK) return st;
+  }
+  b->Tv = s->lin_tv;
+  b->F0 = s->lin_f0;
+  b->F1 = s->lin_f1;
+  return DG_OK;
+}
+
+// forward traces of the linearisation state (into s->T)
+void fwd_traces(dg_solver *s, double *u) {
+  run(s, K_TRACE, [&] { s->ops->trace(s->ctx, u); });
+}
+
+// dout = ca dun + cb dus + ccdt (dL/du dus + dL/db db), linearised at us
+void tl_stage(dg_solver *s, double *us, const double *dus, const double *db, const double *dun,
+              double *dout, double ca, double cb, double ccdt, const LinBufs &lb) {
+  fwd_traces(s, us);
+  dg::Ctx c = s->ctx;
+  c.Fh = lb.F0;
+  run(s, K_TRACE, [&] { dg::lin_trace(c, dus, nullptr, 1.0, lb.Tv); });
+  run(s, K_FACE, [&] { dg::tl_face(c, lb.Tv, lb.F0); });
+  run(s, K_ELEMENT, [&] { dg::tl_element(c, us, dus, db, dun, dout, ca, cb, ccdt); });
+}
+
+// ubar_s = cb obar + ccdt (dL/du)^T obar ; bbar += ccdt (dL/db)^T obar
+void adj_stage(dg_solver *s, double *us, const double *obar, double *ubar_s, double *bbar,
+               double cb, double ccdt, const LinBufs &lb) {
+  fwd_traces(s, us);
+  const dg::Ctx &c = s->ctx;
+  run(s, K_TRACE, [&] { dg::lin_trace(c, obar, s->m.geo + 4 * (size_t)s->m.Kp, ccdt, lb.Tv); });
+  run(s, K_FACE, [&] { dg::adj_face(c, lb.Tv, lb.F0, lb.F1); });
+  run(s, K_ELEMENT, [&] { dg::adj_element(c, us, obar, ubar_s, bbar, lb.F0, lb.F1, cb, ccdt); });
+}
+
+dg_status lin_check(dg_solver *s) {
+  if (s->eq != DG_SHALLOW_WATER)
+    return fail(DG_UNSUPPORTED, "tangent-linear / adjoint operators are for shallow water");
+  if (!dg::lin_supported(s->p)) return fail(DG_UNSUPPORTED, "adjoint orders are p = 1..4");
+  if (s->prm.limiter) return fail(DG_UNSUPPORTED, "adjoint of the limiter is not provided");
+  if (s->has_inout_bc)
+    return fail(DG_UNSUPPORTED, "adjoint supports reflect, transmissive and periodic sides");
+  return DG_OK;
+}
+
+}  // namespace
+
+extern "C" dg_status dg_rhs_tl(dg_solver *s, double t, const double *C, const double *dC,
+                               const double *db, double *dL) {
+  if (!s || !C || !dC || !dL) return fail(DG_BAD_ARG, "null argument");
+  dg_status st = lin_check(s);
+  if (st != DG_OK) return st;
+  CK(cudaSetDevice(s->device));
+  LinBufs lb;
+  if ((st = lin_bufs(s, &lb)) != DG_OK) return st;
+  if ((st = ensure_rk_buffers(s)) != DG_OK) return st;
+  const size_t n = (size_t)s->N * s->np * s->K;
+  const int rows = s->N * s->np;
+  double *u = s->k[0], *du = s->k[1], *out = s->k[2], *dbi = s->k[3];
+  CK(cudaMemcpyAsync(s->ubuf, C, n * sizeof(double), cudaMemcpyHostToDevice, s->st));
+  dg::launch_permute_in(s->st, s->ubuf, u, s->m.perm, rows, s->K, s->m.Kp);
+  CK(cudaMemcpyAsync(s->ubuf, dC, n * sizeof(double), cudaMemcpyHostToDevice, s->st));
+  dg::launch_permute_in(s->st, s->ubuf, du, s->m.perm, rows, s->K, s->m.Kp);
+  const double *dbp = nullptr;
+  if (db) {
+    CK(cudaMemcpyAsync(s->ubuf, db, (size_t)s->np * s->K * sizeof(double),
+                       cudaMemcpyHostToDevice, s->st));
+    dg::launch_permute_in(s->st, s->ubuf, dbi, s->m.perm, s->np, s->K, s->m.Kp);
+    dbp = dbi;
+  }
+  (void)t;
+  tl_stage(s, u, du, dbp, nullptr, out, 0.0, 0.0, 1.0, lb);
+  dg::launch_permute_out(s->st, out, s->ubuf, s->m.perm, rows, s->K, s->m.Kp);
+  CK(cudaMemcpyAsync(dL, s->ubuf, n * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+  collect_profile(s);
+  return sync_check(s);
+}
+
+extern "C" dg_status dg_rhs_adjoint(dg_solver *s, double t, const double *C, const double *Lbar,
+                                    double *Cbar, double *bbar) {
+  if (!s || !C || !Lbar || !Cbar) return fail(DG_BAD_ARG, "null argument");
+  dg_status st = lin_check(s);
+  if (st != DG_OK) return st;
+  CK(cudaSetDevice(s->device));
+  LinBufs lb;
+  if ((st = lin_bufs(s, &lb)) != DG_OK) return st;
+  if ((st = ensure_rk_buffers(s)) != DG_OK) return st;
+  const size_t n = (size_t)s->N * s->np * s->K;
+  const int rows = s->N * s->np;
+  double *u = s->k[0], *lb_in = s->k[1], *out = s->k[2], *bb = s->k[3];
+  CK(cudaMemcpyAsync(s->ubuf, C, n * sizeof(double), cudaMemcpyHostToDevice, s->st));
+  dg::launch_permute_in(s->st, s->ubuf, u, s->m.perm, rows, s->K, s->m.Kp);
+  CK(cudaMemcpyAsync(s->ubuf, Lbar, n * sizeof(double), cudaMemcpyHostToDevice, s->st));
+  dg::launch_permute_in(s->st, s->ubuf, lb_in, s->m.perm, rows, s->K, s->m.Kp);
+  CK(cudaMemsetAsync(bb, 0, (size_t)s->np * s->m.Kp * sizeof(double), s->st));
+  (void)t;
+  adj_stage(s, u, lb_in, out, bb, 0.0, 1.0, lb);
+  dg::launch_permute_out(s->st, out, s->ubuf, s->m.perm, rows, s->K, s->m.Kp);
+  CK(cudaMemcpyAsync(Cbar, s->ubuf, n * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+  if (bbar) {
+    CK(cudaStreamSynchronize(s->st));
+    dg::launch_permute_out(s->st, bb, s->ubuf, s->m.perm, s->np, s->K, s->m.Kp);
+    CK(cudaMemcpyAsync(bbar, s->ubuf, (size_t)s->np * s->K * sizeof(double),
+                       cudaMemcpyDeviceToHost, s->st));
+  }
+  collect_profile(s);
+  return sync_check(s);
+}
+
+// ---- the time-stepping adjoint with checkpoints ------------------------------
+struct dg_adjoint {
+  dg_solver *s = nullptr;
+  int nrec = 0, nsteps = 0, every = 1, ckpt = 50;
+  double dt = 0, t0 = 0;
+  int *rec_el = nullptr;
+  double *rec_phi = nullptr, *samples = nullptr, *sbar = nullptr;
+  std::vector<double *> cks;                  // checkpoints u^{k ckpt}
+  std::vector<double *> seg;                  // 3 ckpt states of a segment: u^n, u1, u2
+  double *ub = nullptr, *ub1 = nullptr, *ub2 = nullptr, *acc = nullptr, *bbar = nullptr;
+  double *du = nullptr, *dw = nullptr, *dbi = nullptr;
+  std::vector<void *> mem;
+};
+
+namespace {
+template <class T>
+dg_status amalloc(dg_adjoint *a, T **p, size_t n) {
+  void *q = nullptr;
+  cudaError_t e = cudaMalloc(&q, (n ? n : 1) * sizeof(T));
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+  a->mem.push_back(q);
+  *p = static_cast<T *>(q);
+  return DG_OK;
+}
+
+// one SSP-RK3 step of fixed dt through the unfused stages; keeps the stage
+// inputs u1, u2 when given (bit-identical to dg_step's fused stages)
+void plain_step(dg_solver *s, double *u1keep, double *u2keep) {
+  const size_t bytes = s->ndof_p * sizeof(double);
+  const double *dt = &s->ds->dt;
+  stage(s, s->U, nullptr, s->W, 0.0, 1.0, 1.0, 0.0, dt);
+  if (u1keep) cudaMemcpyAsync(u1keep, s->W, bytes, cudaMemcpyDeviceToDevice, s->st);
+  stage(s, s->W, s->U, s->W, 0.75, 0.25, 0.25, 1.0, dt);
+  if (u2keep) cudaMemcpyAsync(u2keep, s->W, bytes, cudaMemcpyDeviceToDevice, s->st);
+  stage(s, s->W, s->U, s->U, 1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0, 0.5, dt);
+  run(s, K_CFL, [&] { dg::launch_advance_t(s->st, s->ds); });
+}
+
+dg_status set_fixed_dt(dg_solver *s, double t, double dt) {
+  dg::DevScalars h{};
+  h.t = t;
+  h.dt = dt;
+  h.one = 1.0;
+  h.dmin = s->dmin;
+  h.cfl = s->prm.cfl;
+  h.fixed_dt = dt;
+  return set_scalar(s, 0, &h, sizeof h);
+}
+}  // namespace
+
+extern "C" dg_status dg_adjoint_create(dg_solver *s, int nrec, const double *rx,
+                                       const double *ry, dg_adjoint **out) {
+  if (!s || !out || nrec < 0 || (nrec && (!rx || !ry))) return fail(DG_BAD_ARG, "bad arguments");
+  *out = nullptr;
+  dg_status st = lin_check(s);
+  if (st != DG_OK) return st;
+  CK(cudaSetDevice(s->device));
+  dg_adjoint *a = new dg_adjoint();
+  a->s = s;
+  a->nrec = nrec;
+  // locate receivers: element containing the point, reference coordinates
+  std::vector<int> inv(s->K);
+  std::vector<int> perm(s->K);
+  CK(cudaMemcpy(perm.data(), s->m.perm, sizeof(int) * s->K, cudaMemcpyDeviceToHost));
+  for (int e = 0; e < s->K; e++) inv[perm[e]] = e;
+  std::vector<int> el(nrec);
+  std::vector<double> phi((size_t)nrec * s->np);
+  for (int r = 0; r < nrec; r++) {
+    int found = -1;
+    double rr = 0, ss = 0;
+    for (int o = 0; o < s->K && found < 0; o++) {
+      const double *V = s->mesh_v.data() + (size_t)6 * o;
+      double xr = V[2] - V[0], xs = V[4] - V[0], yr = V[3] - V[1], ys = V[5] - V[1];
+      double J = xr * ys - xs * yr, dx = rx[r] - V[0], dy = ry[r] - V[1];
+      double a1 = (ys * dx - xs * dy) / J, a2 = (-yr * dx + xr * dy) / J;
+      const double tol = -1e-12;
+      if (a1 >= tol && a2 >= tol && a1 + a2 <= 1 - tol) {
+        found = o;
+        rr = a1;
+        ss = a2;
+      }
+    }
+    if (found < 0) {
+      delete a;
+      return fail(DG_BAD_ARG, "receiver " + std::to_string(r) + " lies outside the mesh");
+    }
+    el[r] = inv[found];
+    for (int i = 0; i < s->np; i++) {
+      long double v = 0;
+      for (int m = 0; m <= i; m++) {
+        long double term = DG_COEF[i][m];
+        for (int k = 0; k < DG_MONO[m][0]; k++) term *= rr;
+        for (int k = 0; k < DG_MONO[m][1]; k++) term *= ss;
+        v += term;
+      }
+      phi[(size_t)r * s->np + i] = (double)v;
+    }
+  }
+  if ((st = amalloc(a, &a->rec_el, (size_t)nrec)) != DG_OK) return st;
+  if ((st = amalloc(a, &a->rec_phi, (size_t)nrec * s->np)) != DG_OK) return st;
+  if (nrec) {
+    CK(cudaMemcpy(a->rec_el, el.data(), sizeof(int) * nrec, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(a->rec_phi, phi.data(), sizeof(double) * phi.size(), cudaMemcpyHostToDevice));
+  }
+  *out = a;
+  return DG_OK;
+}
+
+extern "C" void dg_adjoint_destroy(dg_adjoint *a) {
+  if (!a) return;
+  cudaSetDevice(a->s->device);
+  cudaStreamSynchronize(a->s->st);
+  for (void *p : a->mem) cudaFree(p);
+  delete a;
+}
+
+// forward run from the solver's state: nsteps SSP-RK3 steps of fixed dt,
+// h sampled at the receivers after every `every` steps, the state saved
+// every `ckpt` steps; samples = nsteps/every x nrec
+extern "C" dg_status dg_adjoint_forward(dg_adjoint *a, int nsteps, double dt, int every,
+                                        int ckpt, double t0, double *samples) {
+  if (!a || nsteps <= 0 || !(dt > 0) || every <= 0 || ckpt <= 0)
+    return fail(DG_BAD_ARG, "bad forward arguments");
+  dg_solver *s = a->s;
+  CK(cudaSetDevice(s->device));
+  dg_status st;
+  const int nck = (nsteps + ckpt - 1) / ckpt, nsamp = nsteps / every;
+  if (a->nsteps != nsteps || a->ckpt != ckpt || a->every != every || a->cks.empty()) {
+    for (double *p : a->cks) {
+      cudaFree(p);
+      a->mem.erase(std::find(a->mem.begin(), a->mem.end(), (void *)p));
+    }
+    a->cks.assign(nck, nullptr);
+    for (int k = 0; k < nck; k++)
+      if ((st = amalloc(a, &a->cks[k], s->ndof_p)) != DG_OK) return st;
+    for (double *p : a->seg) {
+      cudaFree(p);
+      a->mem.erase(std::find(a->mem.begin(), a->mem.end(), (void *)p));
+    }
+    a->seg.assign(3 * (size_t)ckpt, nullptr);
+    for (auto &p : a->seg)
+      if ((st = amalloc(a, &p, s->ndof_p)) != DG_OK) return st;
+    if (!a->samples) {
+      // (re)sized below
+    }
+  }
+  if (a->samples) {
+    cudaFree(a->samples);
+    a->mem.erase(std::find(a->mem.begin(), a->mem.end(), (void *)a->samples));
+    cudaFree(a->sbar);
+    a->mem.erase(std::find(a->mem.begin(), a->mem.end(), (void *)a->sbar));
+  }
+  if ((st = amalloc(a, &a->samples, (size_t)std::max(nsamp, 1) * std::max(a->nrec, 1))) != DG_OK)
+    return st;
+  if ((st = amalloc(a, &a->sbar, (size_t)std::max(nsamp, 1) * std::max(a->nrec, 1))) != DG_OK)
+    return st;
+  a->nsteps = nsteps;
+  a->every = every;
+  a->ckpt = ckpt;
+  a->dt = dt;
+  a->t0 = t0;
+  if ((st = set_fixed_dt(s, t0, dt)) != DG_OK) return st;
+  const size_t bytes = s->ndof_p * sizeof(double);
+  for (int n = 0; n < nsteps; n++) {
+    if (n % ckpt == 0)
+      CK(cudaMemcpyAsync(a->cks[n / ckpt], s->U, bytes, cudaMemcpyDeviceToDevice, s->st));
+    plain_step(s, nullptr, nullptr);
+    if ((n + 1) % every == 0)
+      dg::launch_sample(s->st, s->U, a->rec_el, a->rec_phi, a->nrec, s->np, s->m.Kp,
+                        a->samples + (size_t)((n + 1) / every - 1) * a->nrec);
+  }
+  if (samples && nsamp && a->nrec)
+    CK(cudaMemcpyAsync(samples, a->samples, sizeof(double) * nsamp * a->nrec,
+                       cudaMemcpyDeviceToHost, s->st));
+  collect_profile(s);
+  return sync_check(s);
+}
+
+// gradients of sum_k,r sbar[k][r] * sample[k][r] with respect to the initial
+// state (all variables, [var][mode][elem]) and the bed modes ([mode][elem]);
+// the forward run must have been made by dg_adjoint_forward
+extern "C" dg_status dg_adjoint_backward(dg_adjoint *a, const double *sbar, double *grad_u0,
+                                         double *grad_b) {
+  if (!a || !sbar || a->cks.empty()) return fail(DG_BAD_ARG, "no forward run to differentiate");
+  dg_solver *s = a->s;
+  CK(cudaSetDevice(s->device));
+  dg_status st;
+  LinBufs lb;
+  if ((st = lin_bufs(s, &lb)) != DG_OK) return st;
+  const size_t bytes = s->ndof_p * sizeof(double);
+  if (!a->ub) {
+    if ((st = amalloc(a, &a->ub, s->ndof_p)) != DG_OK) return st;
+    if ((st = amalloc(a, &a->ub1, s->ndof_p)) != DG_OK) return st;
+    if ((st = amalloc(a, &a->ub2, s->ndof_p)) != DG_OK) return st;
+    if ((st = amalloc(a, &a->acc, s->ndof_p)) != DG_OK) return st;
+    if ((st = amalloc(a, &a->bbar, (size_t)s->np * s->m.Kp)) != DG_OK) return st;
+  }
+  const int nsamp = a->nsteps / a->every;
+  if (nsamp && a->nrec)
+    CK(cudaMemcpyAsync(a->sbar, sbar, sizeof(double) * nsamp * a->nrec, cudaMemcpyHostToDevice,
+                       s->st));
+  CK(cudaMemsetAsync(a->ub, 0, bytes, s->st));
+  CK(cudaMemsetAsync(a->bbar, 0, (size_t)s->np * s->m.Kp * sizeof(double), s->st));
+  const int n = (int)s->ndof_p;
+  const double dt = a->dt;
+  const int nck = (int)a->cks.size();
+  for (int k = nck - 1; k >= 0; k--) {
+    const int n0 = k * a->ckpt, n1 = std::min(n0 + a->ckpt, a->nsteps);
+    // recompute the segment, keeping u^n, u1, u2 of every step
+    CK(cudaMemcpyAsync(s->U, a->cks[k], bytes, cudaMemcpyDeviceToDevice, s->st));
+    if ((st = set_fixed_dt(s, a->t0 + n0 * dt, dt)) != DG_OK) return st;
+    for (int m = n0; m < n1; m++) {
+      const int j = m - n0;
+      CK(cudaMemcpyAsync(a->seg[3 * j], s->U, bytes, cudaMemcpyDeviceToDevice, s->st));
+      plain_step(s, a->seg[3 * j + 1], a->seg[3 * j + 2]);
+    }
+    for (int m = n1 - 1; m >= n0; m--) {
+      const int j = m - n0;
+      if ((m + 1) % a->every == 0)  // adjoint of the sample taken from u^{m+1}
+        dg::launch_sample_adj(s->st, a->ub, a->rec_el, a->rec_phi, a->nrec, s->np, s->m.Kp,
+                              a->sbar + (size_t)((m + 1) / a->every - 1) * a->nrec);
+      double *un = a->seg[3 * j], *u1 = a->seg[3 * j + 1], *u2 = a->seg[3 * j + 2];
+      // u^{n+1} = 1/3 u^n + 2/3 u2 + 2/3 dt L(u2)
+      adj_stage(s, u2, a->ub, a->ub2, a->bbar, 2.0 / 3.0, 2.0 / 3.0 * dt, lb);
+      dg::launch_axpby(s->st, n, 1.0 / 3.0, a->ub, 0.0, a->acc);
+      // u2 = 3/4 u^n + 1/4 u1 + 1/4 dt L(u1)
+      adj_stage(s, u1, a->ub2, a->ub1, a->bbar, 0.25, 0.25 * dt, lb);
+      dg::launch_axpby(s->st, n, 0.75, a->ub2, 1.0, a->acc);
+      // u1 = u^n + dt L(u^n)
+      adj_stage(s, un, a->ub1, a->ub, a->bbar, 1.0, dt, lb);
+      dg::launch_axpby(s->st, n, 1.0, a->acc, 1.0, a->ub);
+    }
+  }
+  const int rows = s->N * s->np;
+  if (grad_u0) {
+    dg::launch_permute_out(s->st, a->ub, s->ubuf, s->m.perm, rows, s->K, s->m.Kp);
+    CK(cudaMemcpyAsync(grad_u0, s->ubuf, sizeof(double) * rows * s->K, cudaMemcpyDeviceToHost,
+                       s->st));
+    CK(cudaStreamSynchronize(s->st));
+  }
+  if (grad_b) {
+    dg::launch_permute_out(s->st, a->bbar, s->ubuf, s->m.perm, s->np, s->K, s->m.Kp);
+    CK(cudaMemcpyAsync(grad_b, s->ubuf, sizeof(double) * s->np * s->K, cudaMemcpyDeviceToHost,
+                       s->st));
+  }
+  // leave the solver at the final state of the forward run
+  CK(cudaMemcpyAsync(s->U, a->cks[nck - 1], bytes, cudaMemcpyDeviceToDevice, s->st));
+  if ((st = set_fixed_dt(s, a->t0 + (nck - 1) * a->ckpt * dt, dt)) != DG_OK) return st;
+  for (int m = (nck - 1) * a->ckpt; m < a->nsteps; m++) plain_step(s, nullptr, nullptr);
+  collect_profile(s);
+  return sync_check(s);
+}
+
+// tangent-linear run: directional derivative of the samples along (du0, db)
+// from the initial state of the last dg_adjoint_forward
+extern "C" dg_status dg_adjoint_tangent(dg_adjoint *a, const double *du0, const double *db,
+                                        double *dsamples) {
+  if (!a || a->cks.empty()) return fail(DG_BAD_ARG, "no forward run to differentiate");
+  dg_solver *s = a->s;
+  CK(cudaSetDevice(s->device));
+  dg_status st;
+  LinBufs lb;
+  if ((st = lin_bufs(s, &lb)) != DG_OK) return st;
+  if (!a->du) {
+    if ((st = amalloc(a, &a->du, s->ndof_p)) != DG_OK) return st;
+    if ((st = amalloc(a, &a->dw, s->ndof_p)) != DG_OK) return st;
+    if ((st = amalloc(a, &a->dbi, (size_t)s->np * s->m.Kp)) != DG_OK) return st;
+  }
+  const size_t bytes = s->ndof_p * sizeof(double);
+  const int rows = s->N * s->np;
+  CK(cudaMemsetAsync(a->du, 0, bytes, s->st));
+  if (du0) {
+    CK(cudaMemcpyAsync(s->ubuf, du0, sizeof(double) * rows * s->K, cudaMemcpyHostToDevice,
+                       s->st));
+    dg::launch_permute_in(s->st, s->ubuf, a->du, s->m.perm, rows, s->K, s->m.Kp);
+  }
+  const double *dbp = nullptr;
+  if (db) {
+    CK(cudaStreamSynchronize(s->st));
+    CK(cudaMemcpyAsync(s->ubuf, db, sizeof(double) * s->np * s->K, cudaMemcpyHostToDevice,
+                       s->st));
+    dg::launch_permute_in(s->st, s->ubuf, a->dbi, s->m.perm, s->np, s->K, s->m.Kp);
+    dbp = a->dbi;
+  }
+  CK(cudaMemcpyAsync(s->U, a->cks[0], bytes, cudaMemcpyDeviceToDevice, s->st));
+  if ((st = set_fixed_dt(s, a->t0, a->dt)) != DG_OK) return st;
+  const double dt = a->dt;
+  const double *dtp = &s->ds->dt;
+  for (int m = 0; m < a->nsteps; m++) {
+    // the tangent stage reads the stage input before the forward stage overwrites it
+    tl_stage(s, s->U, a->du, dbp, nullptr, a->dw, 0.0, 1.0, dt, lb);
+    stage(s, s->U, nullptr, s->W, 0.0, 1.0, 1.0, 0.0, dtp);
+    tl_stage(s, s->W, a->dw, dbp, a->du, a->dw, 0.75, 0.25, 0.25 * dt, lb);
+    stage(s, s->W, s->U, s->W, 0.75, 0.25, 0.25, 1.0, dtp);
+    tl_stage(s, s->W, a->dw, dbp, a->du, a->du, 1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0 * dt, lb);
+    stage(s, s->W, s->U, s->U, 1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0, 0.5, dtp);
+    run(s, K_CFL, [&] { dg::launch_advance_t(s->st, s->ds); });
+    if ((m + 1) % a->every == 0)
+      dg::launch_sample(s->st, a->du, a->rec_el, a->rec_phi, a->nrec, s->np, s->m.Kp,
+                        a->sbar + (size_t)((m + 1) / a->every - 1) * a->nrec);
+  }
+  const int nsamp = a->nsteps / a->every;
+  if (dsamples && nsamp && a->nrec)
+    CK(cudaMemcpyAsync(dsamples, a->sbar, sizeof(double) * nsamp * a->nrec,
+                       cudaMemcpyDeviceToHost, s->st));
+  collect_profile(s);
+  return sync_check(s);
 }
 
 extern "C" dg_status dg_eval_vertices(dg_solver *s, int var, double *uv) {

@@ -200,6 +200,36 @@ dg_status dg_batch_autotune(dg_batch *b, int *block);
 long long dg_batch_launches(const dg_batch *b);
 void dg_batch_destroy(dg_batch *b);
 
+/* ---- derivatives (shallow water, p = 1..4, no limiter; reflect,
+ * transmissive and periodic sides; no reference counterpart) -------------
+ * Tangent-linear right-hand side: dL = dL/du dC + dL/db db (db may be NULL)
+ * and its adjoint: Cbar = (dL/du)^T Lbar, bbar = (dL/db)^T Lbar.  Arrays in
+ * the reference layout, .pmsh order; the flux Jacobians are hand-derived
+ * (Rusanov: the branch of the max taken at C). */
+dg_status dg_rhs_tl(dg_solver *s, double t, const double *C, const double *dC, const double *db,
+                    double *dL);
+dg_status dg_rhs_adjoint(dg_solver *s, double t, const double *C, const double *Lbar,
+                         double *Cbar, double *bbar);
+
+/* Discrete adjoint of SSP-RK3 time stepping with a fixed dt.  Samples are
+ * the water height h at receiver points (rx, ry) after every `every` steps.
+ * dg_adjoint_forward runs nsteps from the solver's current state and bed,
+ * keeping the state every `ckpt` steps; dg_adjoint_backward recomputes each
+ * segment from its checkpoint and sweeps back, returning the gradients of
+ * sum_k,r sbar[k][r] sample[k][r] with respect to the initial state
+ * ([var][mode][elem]) and the bed modes ([mode][elem]); dg_adjoint_tangent
+ * returns the directional derivative of the samples along (du0, db). */
+typedef struct dg_adjoint dg_adjoint;
+dg_status dg_adjoint_create(dg_solver *s, int nrec, const double *rx, const double *ry,
+                            dg_adjoint **out);
+dg_status dg_adjoint_forward(dg_adjoint *a, int nsteps, double dt, int every, int ckpt,
+                             double t0, double *samples);
+dg_status dg_adjoint_backward(dg_adjoint *a, const double *sbar, double *grad_u0,
+                              double *grad_b);
+dg_status dg_adjoint_tangent(dg_adjoint *a, const double *du0, const double *db,
+                             double *dsamples);
+void dg_adjoint_destroy(dg_adjoint *a);
+
 /* Timing of the solver's own kernels (CUDA events around each launch on the
  * solver stream).  When enabled, dg_step launches kernels directly instead
  * of replaying a CUDA graph. */
