@@ -71,6 +71,7 @@ def _declare(L):
         "dg_params_default": (None, [C.POINTER(Params)]),
         "dg_mesh_read_pmsh": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
         "dg_mesh_write_pmsh": (C.c_int, [C.c_void_p, C.c_char_p]),
+        "dg_mesh_read_gmsh": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
         "dg_mesh_from_arrays": (C.c_int, [C.c_int, _dp, _ip, C.c_int, _dp, _ip,
                                           C.POINTER(C.c_void_p)]),
         "dg_mesh_get_arrays": (C.c_int, [C.c_void_p, _dp, _ip, _dp, _ip]),
@@ -102,6 +103,9 @@ def _declare(L):
         "dg_kernel_launches": (C.c_longlong, [C.c_void_p]),
         "dg_measure_fp64_peak": (C.c_int, [C.c_int, _dp]),
         "dg_eval_vertices": (C.c_int, [C.c_void_p, C.c_int, _dp]),
+        "dg_eval_vertices_view": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, _dp]),
+        "dg_save_checkpoint": (C.c_int, [C.c_void_p, C.c_char_p, C.c_double]),
+        "dg_load_checkpoint": (C.c_int, [C.c_void_p, C.c_char_p, _dp]),
         "dg_set_bathymetry": (C.c_int, [C.c_void_p, _dp]),
         "dg_bathymetry_project": (C.c_int, [C.c_void_p, C.c_int, _dp]),
         "dg_get_bathymetry": (C.c_int, [C.c_void_p, _dp]),
@@ -251,6 +255,14 @@ class Mesh:
         return cls(h)
 
     @classmethod
+    def read_gmsh(cls, path):
+        """Gmsh ASCII 2.x .msh, converted as genmesh.py converts it."""
+        L = load_library()
+        h = C.c_void_p()
+        _check(L.dg_mesh_read_gmsh(os.fsencode(path), C.byref(h)))
+        return cls(h)
+
+    @classmethod
     def square(cls, nx, ny, box=(0.0, 1.0, 0.0, 1.0), jitter=0.0, seed=0,
                bc=(PERIODIC, PERIODIC, PERIODIC, PERIODIC)):
         L = load_library()
@@ -390,6 +402,31 @@ class Solver:
         shape (3, K) (eval_u, conserv_kernels.cu:1284)."""
         out = np.empty((3, self.K))
         _check(self._L.dg_eval_vertices(self._h, var, _dptr(out)))
+        return out
+
+    def save_checkpoint(self, path, t):
+        """Binary state (+ bed) with the time t and a checksum."""
+        _check(self._L.dg_save_checkpoint(self._h, os.fsencode(path), t))
+
+    def load_checkpoint(self, path):
+        """Restore a checkpoint written for this equation, order and mesh;
+        returns its time."""
+        t = np.zeros(1)
+        _check(self._L.dg_load_checkpoint(self._h, os.fsencode(path), _dptr(t)))
+        return float(t[0])
+
+    def plot_exact(self, var, t):
+        """The problem's exact solution of `var` at the vertices at time t,
+        shape (3, K) (plot_exact, conserv_kernels.cu:1310)."""
+        out = np.empty((3, self.K))
+        _check(self._L.dg_eval_vertices_view(self._h, var, 1, t, _dptr(out)))
+        return out
+
+    def plot_error(self, var, t):
+        """Solution minus exact solution of `var` at the vertices, shape (3, K)
+        (plot_error, conserv_kernels.cu:1334)."""
+        out = np.empty((3, self.K))
+        _check(self._L.dg_eval_vertices_view(self._h, var, 2, t, _dptr(out)))
         return out
 
     def set_bathymetry(self, b):

@@ -1,7 +1,7 @@
 // dg_cli.cpp -- `dgcuda`, the command line of the reference's run_dgcuda
 // (src/2d/conservation/main.cu:481-974) on top of the C ABI in dg.h.
 //
-//   dgcuda [OPTIONS] MESH
+//   dgcuda [OPTIONS] MESH        (.pmsh, or a Gmsh 2.x .msh converted on the fly)
 //     -n p        order of the polynomial approximation (0..5)
 //     -t steps    number of time steps
 //     -T time     end time
@@ -21,6 +21,8 @@
 //     --gamma g  --gravity g  --velocity ax,ay  --mu m  --eps e
 //     --prm a,b,...    problem parameters
 //     -o DIR           output directory (default "output")
+//     --restart FILE   start from a checkpoint (state, bed and time)
+//     --checkpoint FILE  write a checkpoint at the end
 // Like the reference it writes the final vertex values of U0 to
 // DIR/U0-final.pos (write_U, main.cu:69-116) and, with -e, prints
 // "L2 U<n> error     = %e".
@@ -52,7 +54,7 @@ void usage() {
       "          [--eq advection|euler|shallowwater|maxwell] [--problem NAME]\n"
       "          [--scheme rk4|rk2|ssprk3] [--limiter] [--cfl X] [--gamma G]\n"
       "          [--gravity G] [--velocity AX,AY] [--mu M] [--eps E] [--prm A,B,..]\n"
-      "          [-o DIR]\n");
+      "          [-o DIR] [--restart FILE] [--checkpoint FILE]\n");
 }
 
 std::vector<double> parse_list(const char *s) {
@@ -99,6 +101,7 @@ int main(int argc, char **argv) {
   int benchmark = 0, limiter = 0;
   double endtime = -1, tol = 0, cfl = -1;
   std::string eq_name = "euler", problem = "none", scheme_name = "rk4", outdir = "output";
+  std::string restart, checkpoint;
   dg_params prm;
   dg_params_default(&prm);
   if (argc < 2) {
@@ -155,6 +158,8 @@ int main(int argc, char **argv) {
       auto v = parse_list(next());
       for (size_t k = 0; k < v.size() && k < 8; k++) prm.prm[k] = v[k];
     } else if (a == "-o") outdir = next();
+    else if (a == "--restart") restart = next();
+    else if (a == "--checkpoint") checkpoint = next();
     else {
       std::fprintf(stderr, "unknown option %s\n", a.c_str());
       usage();
@@ -183,7 +188,10 @@ int main(int argc, char **argv) {
   prm.limiter = limiter;
 
   dg_mesh *mesh = nullptr;
-  if (dg_mesh_read_pmsh(mesh_path, &mesh) != DG_OK) return fail("reading the mesh");
+  const size_t plen = std::strlen(mesh_path);
+  const bool gmsh = plen > 4 && !std::strcmp(mesh_path + plen - 4, ".msh");
+  if ((gmsh ? dg_mesh_read_gmsh(mesh_path, &mesh) : dg_mesh_read_pmsh(mesh_path, &mesh)) != DG_OK)
+    return fail("reading the mesh");
   int K = 0, S = 0;
   dg_mesh_sizes(mesh, &K, &S);
   std::vector<double> V((size_t)6 * K);
@@ -203,8 +211,10 @@ int main(int argc, char **argv) {
   mkdir(outdir.c_str(), 0755);
   if (video > 0) mkdir((outdir + "/video").c_str(), 0755);
 
-  auto start = std::chrono::steady_clock::now();
   double t = 0.0;
+  if (!restart.empty() && dg_load_checkpoint(s, restart.c_str(), &t) != DG_OK)
+    return fail("reading the checkpoint");
+  auto start = std::chrono::steady_clock::now();
   int steps = 0, vid = 0;
   const bool per_step = verbose || video > 0 || convergence;
   if (!per_step) {
@@ -261,6 +271,8 @@ int main(int argc, char **argv) {
     for (int n = 0; n < N; n++) std::printf("L2 U%i error     = %e\n", n, err[n]);
   }
   if (!write_pos(s, V, K, 0, outdir + "/U0-final.pos")) return fail("writing output");
+  if (!checkpoint.empty() && dg_save_checkpoint(s, checkpoint.c_str(), t) != DG_OK)
+    return fail("writing the checkpoint");
   std::printf("t = %.15g after %d steps\n", t, steps);
   dg_solver_destroy(s);
   dg_mesh_destroy(mesh);

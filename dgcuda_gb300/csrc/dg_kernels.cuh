@@ -395,6 +395,18 @@ __global__ void __launch_bounds__(kMaxBlock) k_limit(const __grid_constant__ Tab
   }
 }
 
+// Order-preserving integer view of a double: for non-NaN x, y,
+// x < y  <=>  order_key(x) < order_key(y) (with -0 just below +0).  Negative
+// values get their 63 low bits flipped, so signed 64-bit comparison follows
+// the real line.  The map is its own inverse.
+__device__ __forceinline__ long long order_key(double x) {
+  const long long b = __double_as_longlong(x);
+  return b ^ (long long)((unsigned long long)(b >> 63) >> 1);
+}
+__device__ __forceinline__ double from_order_key(long long k) {
+  return __longlong_as_double(k ^ (long long)((unsigned long long)(k >> 63) >> 1));
+}
+
 // ---------------------------------------------------------------------------
 // The same limiter reading the edge traces k_element<TR> left in T instead of
 // re-evaluating them; a limited variable's traces are rebuilt from its
@@ -422,13 +434,18 @@ __device__ __forceinline__ void limit_tr_body(const Tab<P> &tab, const EqP &q, d
                  m2 = __dmul_rn(row[nb2], phi0);
     const double Umin = fmin(Uc, fmin(m0, fmin(m1, m2)));
     const double Umax = fmax(Uc, fmax(m0, fmax(m1, m2)));
-    double up = 0.0, dn = 0.0;
+    // max_k (T_k - Uc) = max_k T_k - Uc exactly (rounding is monotonic), so
+    // the extremes of the edge values are found first, on the integer pipe
+    // (order_key), and each is subtracted once
+    long long kmax = order_key(Te[n]), kmin = kmax;
 #pragma unroll
-    for (int k = 0; k < 3 * N1; k++) {
-      const double d = Te[k * N + n] - Uc;
-      up = fmax(up, d);
-      dn = fmax(dn, -d);
+    for (int k = 1; k < 3 * N1; k++) {
+      const long long kk = order_key(Te[k * N + n]);
+      kmax = max(kmax, kk);
+      kmin = min(kmin, kk);
     }
+    const double up = fmax(0.0, from_order_key(kmax) - Uc);
+    const double dn = fmax(0.0, Uc - from_order_key(kmin));
     double alpha = 1.0;
     if (up > 0.0) alpha = fmin(alpha, (Uc - Umin) / up);
     if (dn > 0.0) alpha = fmin(alpha, (Umax - Uc) / dn);
@@ -602,22 +619,34 @@ __global__ void __launch_bounds__(kBlock) k_l2err(const __grid_constant__ Tab<P>
 }
 
 // ---------------------------------------------------------------------------
-// values of variable `var` at the three vertices (eval_u, conserv_kernels.cu:1284-1307)
+// values of variable `var` at the three vertices: mode 0 the solution
+// (eval_u, conserv_kernels.cu:1284-1307), 1 the exact solution at time t
+// (plot_exact, :1310-1331), 2 solution minus exact (plot_error, :1334-1369;
+// the reference reads basis_vertex with stride 6 there, past the [n_p][3]
+// table, which here is read as the table it is)
 template <class Eq, int P>
 __global__ void __launch_bounds__(kBlock) k_vertex(const __grid_constant__ Tab<P> tab,
+                                                   const __grid_constant__ EqP q,
                                                    const double *__restrict__ u, int var,
+                                                   int mode, double t,
+                                                   const double *__restrict__ vtx,
                                                    double *__restrict__ out, int K, int Kp) {
   constexpr int NP = Tab<P>::NP;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= K) return;
   double c[NP];
 #pragma unroll
-  for (int i = 0; i < NP; i++) c[i] = u[(size_t)(var * NP + i) * Kp + e];
+  for (int i = 0; i < NP; i++) c[i] = mode == 1 ? 0.0 : u[(size_t)(var * NP + i) * Kp + e];
 #pragma unroll
   for (int v = 0; v < 3; v++) {
     double a = 0.0;
 #pragma unroll
     for (int i = 0; i < NP; i++) a += c[i] * tab.V[v][i];
+    if (mode != 0) {
+      double U[4];
+      exact_state(q, U, vtx[(size_t)(2 * v) * Kp + e], vtx[(size_t)(2 * v + 1) * Kp + e], t);
+      a = mode == 1 ? U[var] : a - U[var];
+    }
     out[(size_t)v * Kp + e] = a;
   }
 }
@@ -845,9 +874,9 @@ struct Launch {
     return (int)nblk(c.m.K);
   }
 
-  static void vertex(const Ctx &c, const double *u, int var, double *out) {
-    DG_DISPATCH_P((k_vertex<Eq, P><<<nblk(c.m.K), kBlock, 0, c.st>>>(tab<P>(c), u, var, out,
-                                                                      c.m.K, c.m.Kp)));
+  static void vertex(const Ctx &c, const double *u, int var, int mode, double t, double *out) {
+    DG_DISPATCH_P((k_vertex<Eq, P><<<nblk(c.m.K), kBlock, 0, c.st>>>(
+        tab<P>(c), *c.q, u, var, mode, t, c.m.vtx, out, c.m.K, c.m.Kp)));
   }
 #undef DG_DISPATCH_P
 

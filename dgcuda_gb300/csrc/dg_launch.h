@@ -125,7 +125,7 @@ struct Ops {
   // limit() reading and updating the traces in T (after element_tr)
   void (*limit_tr)(const Ctx &, double *u);
   // values of variable var at the three vertices, rows of Kp: out[v][elem]
-  void (*vertex)(const Ctx &, const double *u, int var, double *out);
+  void (*vertex)(const Ctx &, const double *u, int var, int mode, double t, double *out);
 };
 
 const Ops &ops_advection();

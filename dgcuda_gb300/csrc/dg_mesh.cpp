@@ -410,3 +410,173 @@ extern "C" dg_status dg_mesh_square(int nx, int ny, double x0, double x1, double
   *out = m;
   return DG_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Gmsh ASCII .msh (format 2.2) -> mesh, the conversion genmesh.py performs
+// (genmesh.py:13-315):
+//  * nodes keep their (x, y); line elements (type 1) carry the boundary code
+//    in their first (physical) tag: 10000 -> -1 reflect, 20000 -> -2 outflow,
+//    30000 -> -3 inflow (genmesh.py:166-174), and, as an addition of this
+//    library, 40000 -> -4 transmissive; triangles (type 2) are the elements,
+//    in file order; other element types are skipped;
+//  * sides are created element by element, faces (v1,v2), (v2,v3), (v3,v1):
+//    the first element to visit a side is its left element, the second its
+//    right element with its face number (genmesh.py:86-222);
+//  * boundary sides are then moved to the front, code -1 first, then -2 and
+//    -3, by swapping each one found (in side order) with the next free front
+//    slot (genmesh.py:226-268), and the element -> side links follow.
+// Deliberate differences, where genmesh.py would write an inconsistent
+// mesh: a clockwise triangle is reoriented (its first two vertices swapped)
+// before its sides are made, not only in the written coordinates
+// (genmesh.py:284-288); a side with one element and no tagged line is an
+// error (genmesh.py leaves element 0 as its right neighbour); node numbers
+// need not be consecutive.
+extern "C" dg_status dg_mesh_read_gmsh(const char *path, dg_mesh **out) {
+  using dg::fail;
+  if (!path || !out) return fail(DG_BAD_ARG, "null argument");
+  *out = nullptr;
+  FILE *f = std::fopen(path, "r");
+  if (!f) return fail(DG_IO_ERROR, std::string("cannot open ") + path);
+  struct Closer {
+    FILE *f;
+    ~Closer() { std::fclose(f); }
+  } closer{f};
+  char buf[4096];
+  auto seek = [&](const char *tag) {
+    while (std::fgets(buf, sizeof buf, f))
+      if (std::strncmp(buf, tag, std::strlen(tag)) == 0) return true;
+    return false;
+  };
+  if (!seek("$MeshFormat")) return fail(DG_BAD_MESH, "no $MeshFormat section");
+  double version = 0;
+  int ftype = -1;
+  if (!std::fgets(buf, sizeof buf, f) || std::sscanf(buf, "%lf %d", &version, &ftype) != 2)
+    return fail(DG_BAD_MESH, "bad $MeshFormat line");
+  if (version < 2.0 || version >= 3.0 || ftype != 0)
+    return fail(DG_UNSUPPORTED, "only ASCII Gmsh format 2.x is read");
+  if (!seek("$Nodes")) return fail(DG_BAD_MESH, "no $Nodes section");
+  long nn = 0;
+  if (!std::fgets(buf, sizeof buf, f) || std::sscanf(buf, "%ld", &nn) != 1 || nn <= 0)
+    return fail(DG_BAD_MESH, "bad node count");
+  std::unordered_map<long, int> node_index;
+  std::vector<double> nx(nn), ny(nn);
+  for (long i = 0; i < nn; i++) {
+    long id;
+    double x, y, z;
+    if (!std::fgets(buf, sizeof buf, f) || std::sscanf(buf, "%ld %lf %lf %lf", &id, &x, &y, &z) != 4)
+      return fail(DG_BAD_MESH, "bad node line " + std::to_string(i + 1));
+    node_index[id] = (int)i;
+    nx[i] = x;
+    ny[i] = y;
+  }
+  if (!seek("$Elements")) return fail(DG_BAD_MESH, "no $Elements section");
+  long ne = 0;
+  if (!std::fgets(buf, sizeof buf, f) || std::sscanf(buf, "%ld", &ne) != 1 || ne < 0)
+    return fail(DG_BAD_MESH, "bad element count");
+  auto edge_key = [](int a, int b) {
+    const unsigned lo = (unsigned)std::min(a, b), hi = (unsigned)std::max(a, b);
+    return ((uint64_t)hi << 32) | lo;
+  };
+  std::unordered_map<uint64_t, int> bcode;  // node pair -> boundary code
+  std::vector<int> tri;                      // 3 node indices per element
+  for (long i = 0; i < ne; i++) {
+    if (!std::fgets(buf, sizeof buf, f)) return fail(DG_BAD_MESH, "truncated $Elements");
+    std::vector<long> v;
+    char *p = buf, *end;
+    for (;;) {
+      long x = std::strtol(p, &end, 10);
+      if (end == p) break;
+      v.push_back(x);
+      p = end;
+    }
+    if (v.size() < 3 || (long)v.size() < 3 + v[2])
+      return fail(DG_BAD_MESH, "bad element line " + std::to_string(i + 1));
+    const long type = v[1], ntags = v[2];
+    const size_t n0 = 3 + (size_t)ntags;
+    auto node = [&](size_t k, int *o) {
+      auto it = node_index.find(v[k]);
+      if (it == node_index.end()) return false;
+      *o = it->second;
+      return true;
+    };
+    if (type == 1) {
+      int a, b;
+      if (v.size() < n0 + 2 || !node(n0, &a) || !node(n0 + 1, &b))
+        return fail(DG_BAD_MESH, "bad line element " + std::to_string(v[0]));
+      const long tag = ntags > 0 ? v[3] : 0;
+      const int code = tag == 10000 ? -1 : tag == 20000 ? -2 : tag == 30000 ? -3 : tag == 40000 ? -4 : 0;
+      if (code) bcode[edge_key(a, b)] = code;
+    } else if (type == 2) {
+      int a, b, c;
+      if (v.size() < n0 + 3 || !node(n0, &a) || !node(n0 + 1, &b) || !node(n0 + 2, &c))
+        return fail(DG_BAD_MESH, "bad triangle " + std::to_string(v[0]));
+      const double J = (nx[b] - nx[a]) * (ny[c] - ny[a]) - (nx[c] - nx[a]) * (ny[b] - ny[a]);
+      if (J < 0) std::swap(a, b);
+      tri.push_back(a);
+      tri.push_back(b);
+      tri.push_back(c);
+    }
+  }
+  const int K = (int)(tri.size() / 3);
+  if (K == 0) return fail(DG_BAD_MESH, "no triangles in the mesh");
+  struct Side {
+    int a, b, left, right, lsn, rsn;
+  };
+  std::vector<Side> sides;
+  sides.reserve((size_t)K * 3 / 2 + 16);
+  std::unordered_map<uint64_t, int> smap;
+  for (int e = 0; e < K; e++)
+    for (int k = 0; k < 3; k++) {
+      const int a = tri[3 * e + k], b = tri[3 * e + (k + 1) % 3];
+      const uint64_t key = edge_key(a, b);
+      auto it = smap.find(key);
+      if (it != smap.end()) {
+        Side &s = sides[it->second];
+        if (s.right >= 0 && s.right != INT32_MAX)
+          return fail(DG_BAD_MESH, "a side is shared by more than two triangles");
+        s.right = e;
+        s.rsn = k;
+      } else {
+        smap[key] = (int)sides.size();
+        auto bc = bcode.find(key);
+        sides.push_back({a, b, e, bc != bcode.end() ? bc->second : INT32_MAX, k, 0});
+      }
+    }
+  for (const Side &s : sides)
+    if (s.right == INT32_MAX)
+      return fail(DG_BAD_MESH, "boundary side without a tagged line (10000/20000/30000/40000)");
+  int front = 0;
+  for (int code = -1; code >= -4; code--)
+    for (size_t i = 0; i < sides.size(); i++)
+      if (sides[i].right == code) std::swap(sides[i], sides[front++]);
+  dg_mesh *m = new dg_mesh();
+  m->K = K;
+  m->S = (int)sides.size();
+  for (int k = 0; k < 6; k++) m->V[k].resize(K);
+  for (int k = 0; k < 3; k++) m->es[k].assign(K, -1);
+  for (int e = 0; e < K; e++)
+    for (int v = 0; v < 3; v++) {
+      m->V[2 * v][e] = nx[tri[3 * e + v]];
+      m->V[2 * v + 1][e] = ny[tri[3 * e + v]];
+    }
+  for (int j = 0; j < m->S; j++) {
+    const Side &s = sides[j];
+    m->sx1.push_back(nx[s.a]);
+    m->sy1.push_back(ny[s.a]);
+    m->sx2.push_back(nx[s.b]);
+    m->sy2.push_back(ny[s.b]);
+    m->left.push_back(s.left);
+    m->right.push_back(s.right);
+    m->lsn.push_back(s.lsn);
+    m->rsn.push_back(s.rsn);
+    m->es[s.lsn][s.left] = j;
+    if (s.right >= 0) m->es[s.rsn][s.right] = j;
+  }
+  dg_status st = dg::validate_mesh(*m);
+  if (st != DG_OK) {
+    delete m;
+    return st;
+  }
+  *out = m;
+  return DG_OK;
+}

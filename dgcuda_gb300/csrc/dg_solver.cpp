@@ -8,6 +8,7 @@
 // with float sqrtf, conserv_kernels.cu:412-585) and uploaded once.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <map>
 #include <numeric>
@@ -1561,10 +1562,16 @@ extern "C" dg_status dg_adjoint_tangent(dg_adjoint *a, const double *du0, const 
 }
 
 extern "C" dg_status dg_eval_vertices(dg_solver *s, int var, double *uv) {
+  return dg_eval_vertices_view(s, var, DG_VIEW_SOLUTION, 0.0, uv);
+}
+
+extern "C" dg_status dg_eval_vertices_view(dg_solver *s, int var, int view, double t,
+                                           double *uv) {
   if (!s || !uv) return fail(DG_BAD_ARG, "null argument");
   if (var < 0 || var >= s->N) return fail(DG_BAD_ARG, "variable index out of range");
+  if (view < DG_VIEW_SOLUTION || view > DG_VIEW_ERROR) return fail(DG_BAD_ARG, "unknown view");
   CK(cudaSetDevice(s->device));
-  run(s, K_RK, [&] { s->ops->vertex(s->ctx, s->U, var, s->vbuf); });
+  run(s, K_RK, [&] { s->ops->vertex(s->ctx, s->U, var, view, t, s->vbuf); });
   double *user = s->vbuf + (size_t)3 * s->m.Kp;
   dg::launch_permute_out(s->st, s->vbuf, user, s->m.perm, 3, s->K, s->m.Kp);
   CK(cudaMemcpyAsync(uv, user, (size_t)3 * s->K * sizeof(double), cudaMemcpyDeviceToHost,
@@ -1621,3 +1628,82 @@ SolverView solver_view(dg_solver *s) {
   return v;
 }
 }  // namespace dg
+
+// ---------------------------------------------------------------------------
+// binary checkpoint / restart (the reference has none: its -V output is
+// vertex values only, time_integrator.cu:426-432).  Little-endian file:
+//   "DGCKPT01", int32 eq, p, N, n_p, K, has_bed, double t,
+//   N*n_p*K doubles of state [var][mode][elem] (.pmsh element order),
+//   n_p*K doubles of bed modes when has_bed,
+//   uint64 FNV-1a hash of every byte before it.
+namespace {
+constexpr char kCkptMagic[8] = {'D', 'G', 'C', 'K', 'P', 'T', '0', '1'};
+
+uint64_t fnv1a(uint64_t h, const void *p, size_t n) {
+  const unsigned char *b = static_cast<const unsigned char *>(p);
+  for (size_t i = 0; i < n; i++) h = (h ^ b[i]) * 0x100000001b3ull;
+  return h;
+}
+}  // namespace
+
+extern "C" dg_status dg_save_checkpoint(dg_solver *s, const char *path, double t) {
+  if (!s || !path) return fail(DG_BAD_ARG, "null argument");
+  const size_t n = (size_t)s->N * s->np * s->K, nb = (size_t)s->np * s->K;
+  const int32_t hdr[6] = {(int32_t)s->eq, s->p, s->N, s->np, s->K, s->m.bathy ? 1 : 0};
+  std::vector<double> u(n), b(hdr[5] ? nb : 0);
+  dg_status st = dg_get_state(s, u.data());
+  if (st != DG_OK) return st;
+  if (hdr[5] && (st = dg_get_bathymetry(s, b.data())) != DG_OK) return st;
+  FILE *f = std::fopen(path, "wb");
+  if (!f) return fail(DG_IO_ERROR, std::string("cannot write ") + path);
+  uint64_t h = 0xcbf29ce484222325ull;
+  auto put = [&](const void *p, size_t bytes) {
+    h = fnv1a(h, p, bytes);
+    return std::fwrite(p, 1, bytes, f) == bytes;
+  };
+  bool ok = put(kCkptMagic, 8) && put(hdr, sizeof hdr) && put(&t, sizeof t) &&
+            put(u.data(), n * sizeof(double)) && (b.empty() || put(b.data(), nb * sizeof(double)));
+  ok = ok && std::fwrite(&h, 1, sizeof h, f) == sizeof h;
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? DG_OK : fail(DG_IO_ERROR, std::string("write failed: ") + path);
+}
+
+extern "C" dg_status dg_load_checkpoint(dg_solver *s, const char *path, double *t) {
+  if (!s || !path) return fail(DG_BAD_ARG, "null argument");
+  FILE *f = std::fopen(path, "rb");
+  if (!f) return fail(DG_IO_ERROR, std::string("cannot open ") + path);
+  uint64_t h = 0xcbf29ce484222325ull;
+  auto get = [&](void *p, size_t bytes) {
+    if (std::fread(p, 1, bytes, f) != bytes) return false;
+    h = fnv1a(h, p, bytes);
+    return true;
+  };
+  char magic[8];
+  int32_t hdr[6];
+  double tt = 0;
+  if (!get(magic, 8) || std::memcmp(magic, kCkptMagic, 8) || !get(hdr, sizeof hdr) ||
+      !get(&tt, sizeof tt)) {
+    std::fclose(f);
+    return fail(DG_IO_ERROR, std::string("not a checkpoint file: ") + path);
+  }
+  if (hdr[0] != (int32_t)s->eq || hdr[1] != s->p || hdr[2] != s->N || hdr[3] != s->np ||
+      hdr[4] != s->K || (hdr[5] && s->eq != DG_SHALLOW_WATER)) {
+    std::fclose(f);
+    return fail(DG_BAD_ARG, "checkpoint was written for another equation, order or mesh");
+  }
+  const size_t n = (size_t)s->N * s->np * s->K, nb = (size_t)s->np * s->K;
+  std::vector<double> u(n), b(hdr[5] ? nb : 0);
+  uint64_t stored = 0;
+  bool ok = get(u.data(), n * sizeof(double)) && (b.empty() || get(b.data(), nb * sizeof(double)));
+  const uint64_t computed = h;
+  ok = ok && std::fread(&stored, 1, sizeof stored, f) == sizeof stored;
+  std::fclose(f);
+  if (!ok) return fail(DG_IO_ERROR, std::string("truncated checkpoint: ") + path);
+  if (stored != computed) return fail(DG_IO_ERROR, std::string("checkpoint checksum mismatch: ") + path);
+  dg_status st = dg_set_state(s, u.data());
+  if (st != DG_OK) return st;
+  if (s->eq == DG_SHALLOW_WATER && (st = dg_set_bathymetry(s, hdr[5] ? b.data() : nullptr)) != DG_OK)
+    return st;
+  if (t) *t = tt;
+  return DG_OK;
+}

@@ -88,6 +88,12 @@ void dg_params_default(dg_params *p);
  * (genmesh.py:286-313) */
 dg_status dg_mesh_read_pmsh(const char *path, dg_mesh **out);
 dg_status dg_mesh_write_pmsh(const dg_mesh *m, const char *path);
+/* Gmsh ASCII 2.x .msh -> mesh, as genmesh.py converts it (genmesh.py:13-315):
+ * triangles in file order, sides in first-visit order, boundary sides first
+ * by code; line physical tags 10000/20000/30000 -> -1/-2/-3 (40000 -> -4 is
+ * an addition).  Writing the result with dg_mesh_write_pmsh gives the
+ * .pmsh genmesh.py writes. */
+dg_status dg_mesh_read_gmsh(const char *path, dg_mesh **out);
 /* arrays in .pmsh column order: V = 6*K doubles as V1x[K],V1y[K],V2x[K],
  * V2y[K],V3x[K],V3y[K]; elem_sides = 3*K ints s1[K],s2[K],s3[K];
  * side_xy = 4*S doubles x1[S],y1[S],x2[S],y2[S]; side_elems = 4*S ints
@@ -165,6 +171,22 @@ dg_status dg_l2_error(dg_solver *s, double t, double *err);
  * element e (.pmsh order) -- eval_u + the copies of write_U
  * (conserv_kernels.cu:1284-1307, main.cu:69-116) */
 dg_status dg_eval_vertices(dg_solver *s, int var, double *uv);
+/* the same layout for other views: DG_VIEW_SOLUTION (= dg_eval_vertices),
+ * DG_VIEW_EXACT (the problem's exact solution at time t, plot_exact,
+ * conserv_kernels.cu:1310-1331), DG_VIEW_ERROR (solution - exact,
+ * plot_error, :1334-1369) */
+#define DG_VIEW_SOLUTION 0
+#define DG_VIEW_EXACT 1
+#define DG_VIEW_ERROR 2
+dg_status dg_eval_vertices_view(dg_solver *s, int var, int view, double t, double *uv);
+
+/* binary checkpoint / restart (no reference counterpart: the reference's
+ * output is vertex values only).  The file holds the equation, order,
+ * sizes, the time t, the state in .pmsh order, the shallow-water bed when
+ * one is set, and a checksum; loading into a solver of another equation,
+ * order or mesh size is DG_BAD_ARG, a damaged file DG_IO_ERROR. */
+dg_status dg_save_checkpoint(dg_solver *s, const char *path, double t);
+dg_status dg_load_checkpoint(dg_solver *s, const char *path, double *t);
 
 /* ---- shallow-water bed (the reference's source_term hook,
  * conserv_kernels.cu:1063; its modules define no bed) -----------------------

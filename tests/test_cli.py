@@ -48,3 +48,23 @@ def test_cli_matches_library(dglib, tmp_path):
     uv = s.eval_u(0)
     first = [float(x) for x in re.findall(r"\{([^}]*)\}", lines[1])[0].split(",")]
     np.testing.assert_allclose(first, uv[:, 0], rtol=1e-12)
+
+
+@pytest.mark.gpu
+def test_cli_runs_a_gmsh_file(dglib, tmp_path):
+    """A Gmsh .msh given to the CLI is converted as genmesh.py would and run."""
+    dg = dglib
+    msh = os.path.join(ROOT, "tests", "golden", "gmsh_square6.msh")
+    out = str(tmp_path / "out")
+    r = subprocess.run([CLI, "-n", "1", "-t", "5", "--eq", "advection", "--problem", "adv_sine",
+                        "-o", out, msh], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    mesh = dg.Mesh.read_gmsh(msh)
+    s = dg.Solver(mesh, dg.ADVECTION, 1, problem="adv_sine", cfl=0.5)
+    s.init_conditions()
+    s.step(5, dg.RK4, 0.0)
+    uv = s.eval_u(0)
+    lines = open(os.path.join(out, "U0-final.pos")).read().splitlines()
+    vals = np.array([[float(x) for x in re.findall(r"\{([^}]*)\}", l)[0].split(",")]
+                     for l in lines[1:1 + mesh.K]])
+    np.testing.assert_allclose(vals, uv.T, rtol=0, atol=1e-12)
