@@ -105,6 +105,8 @@ def _declare(L):
         "dg_eval_vertices": (C.c_int, [C.c_void_p, C.c_int, _dp]),
         "dg_eval_vertices_view": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, _dp]),
         "dg_save_checkpoint": (C.c_int, [C.c_void_p, C.c_char_p, C.c_double]),
+        "dg_set_tensor_contractions": (C.c_int, [C.c_void_p, C.c_int]),
+        "dg_get_tensor_contractions": (C.c_int, [C.c_void_p, _ip]),
         "dg_load_checkpoint": (C.c_int, [C.c_void_p, C.c_char_p, _dp]),
         "dg_set_bathymetry": (C.c_int, [C.c_void_p, _dp]),
         "dg_bathymetry_project": (C.c_int, [C.c_void_p, C.c_int, _dp]),
@@ -403,6 +405,18 @@ class Solver:
         out = np.empty((3, self.K))
         _check(self._L.dg_eval_vertices(self._h, var, _dptr(out)))
         return out
+
+    @property
+    def tensor_contractions(self):
+        """True when the fused element stage runs its contractions on the
+        tensor cores (Euler, p = 1..4, default on)."""
+        v = np.zeros(1, dtype=np.int32)
+        _check(self._L.dg_get_tensor_contractions(self._h, _iptr(v)))
+        return bool(v[0])
+
+    @tensor_contractions.setter
+    def tensor_contractions(self, on):
+        _check(self._L.dg_set_tensor_contractions(self._h, int(bool(on))))
 
     def save_checkpoint(self, path, t):
         """Binary state (+ bed) with the time t and a checksum."""

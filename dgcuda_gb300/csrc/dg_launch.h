@@ -58,6 +58,7 @@ struct Ctx {
   double *T = nullptr;            // traces [elem][face][j][var]
   double *Fh = nullptr;           // face fluxes [side][j][var], scaled by len/2 * w_j
   DevScalars *ds = nullptr;       // device scalars
+  const void *oz = nullptr;       // tensor-core tables of order p (null: FP64 contractions)
 };
 
 // one problem of a batched ensemble (device resident)
@@ -130,6 +131,11 @@ struct Ops {
 
 const Ops &ops_advection();
 const Ops &ops_euler();
+// tensor-core element stage (Euler, p = 1..4): table image size, builder
+// from the host Tab<p> image, and the per-device kernel attribute
+size_t oz_tabs_bytes();
+bool oz_build_tabs(int p, const void *tabimg, void *out);
+cudaError_t oz_prepare_euler(int p);
 const Ops &ops_shallow_water();
 const Ops &ops_maxwell();
 

@@ -1,0 +1,599 @@
+// dg_ozaki.cuh -- the element kernel's basis contractions on the tensor
+// cores with FP64 accuracy (exact-slice emulation after Ozaki, Ogita and
+// Oishi, "Error-free transformations of matrix multiplication by using fast
+// routines of matrix multiplication and its applications", Numer. Algorithms
+// 59, 2012; slices held as small integers, as in Ootomo, Ozaki and Yokota,
+// IJHPCA 2024).
+//
+// GB300 runs FP64 FMAs at 2 per SM per cycle and f16 tensor MMAs at ~960
+// multiply-adds per SM per cycle (mma.sync, measured), so the element kernel
+// is bound by its FP64 basis contractions: u(q) = sum_i c_i phi_i(q) at the
+// area points, the projection sum_q (GR_qi g_q + GS_qi h_q), the surface
+// gather sum_fj E_fji F_fj and the next stage's edge traces.  Here each of
+// them runs as exact integer arithmetic on the tensor cores:
+//
+//  * a row of inputs (one element and variable) shares the exponent of its
+//    largest entry; each entry becomes a 53-bit integer X (truncated), and X
+//    is written in 7 balanced base-256 digits d_j in [-128, 127]
+//    (X + 0x80808080808080 has the unsigned digits d_j + 128);
+//  * the table columns are split the same way (on the host);
+//  * every digit pair (i, j) with i + j >= 5 is one f16 MMA with f32
+//    accumulation; pairs of equal weight 256^(i+j) share an accumulator.  A
+//    product is at most 2^14, a weight class has at most 7 pairs, a group
+//    accumulates at most 32 real K slots (p <= 4), so every partial sum is an
+//    integer below 7 * 32 * 2^14 < 2^22 in magnitude: the accumulator starts at 1.5 * 2^23, where
+//    fp32 holds every integer of the window exactly, and the integer is read
+//    back from its bits;
+//  * the 8 weight sums are combined in 64-bit integers and turned into one
+//    double with two exact conversions (a power-of-two bias added to the
+//    integer bits, the bias subtracted in FP64) and one rounding.
+//  The pairs left out (i + j < 5) and the truncation of the inputs bound the
+//  error of each output by about 2^-52 max|x| max|t| times the slot count,
+//  the order of an FP64 dot product's own rounding.
+//
+// Layout: one warp contracts 16 elements (rows g and g + 8 of the MMA, g =
+// lane / 4); the 4 lanes of a quad hold K slots {2t, 2t+1, 2t+8, 2t+9} (t =
+// lane % 4) of both rows, which are the positions 0..3 of the thread.  The
+// D fragment of an MMA gives the thread the output columns at the same
+// positions, so the four contractions chain without moving data: the area
+// points the first one produces are the K slots of the projection, and the
+// modes the projection produces are the K slots of the trace contraction.
+// Items (modes, area points, edge points) fill the positions in the order
+// position 0 of t = 0..3, position 1 of t = 0..3, and so on, so every lane
+// has the same number of real items up to the last position.
+#pragma once
+#include <cstdint>
+
+#include <cuda_fp16.h>
+
+#include "dg_kernels.cuh"
+
+namespace dg {
+namespace oz {
+
+constexpr int kDigits = 7;
+constexpr int kMinPair = 5;                 // digit pairs with i + j >= 5
+constexpr int kWeights = 8;                 // weight classes 12 - (i + j) = 0..7
+constexpr unsigned long long kBias = 0x80808080808080ull;
+constexpr float kAccInit = 12582912.0f;     // 1.5 * 2^23
+constexpr int kAccBits = 0x4B400000;        // its bit pattern
+
+// tables: EVAL (K = modes, N = area points), PROJ (2 K blocks: GR, GS over
+// area points; N = modes), SURF (K = edge points, N = modes), TRACE (K =
+// modes, N = edge points).  Words are the B fragments of each lane:
+// word[digit][kblock][colgroup][lane] = {k 2t..2t+1, k 2t+8..2t+9} of column
+// colgroup * 8 + g, as f16 pairs.
+enum { kEval = 0, kProj = 1, kSurf = 2, kTrace = 3 };
+// word offset of each table: 7 digits x 2 column groups x 32 lanes per K
+// block, K blocks 1, 2, 1, 1
+__host__ __device__ constexpr int word_off(int tab) { return 7 * 2 * 32 * (tab <= 1 ? tab : tab + 1); }
+constexpr int kWords = 7 * 5 * 2 * 32;      // 2240 uint2
+struct Tabs {
+  uint2 w[kWords];
+  int colexp[4][16];                         // biased exponent of each table column
+};
+
+// position p of lane quad index t -> slot (0..15); item index of (p, t)
+__host__ __device__ constexpr int slot_of(int pos, int t) { return pos < 2 ? 2 * t + pos : 2 * t + 8 + (pos - 2); }
+__host__ __device__ constexpr int npos(int items) { return (items + 3) / 4; }
+
+// ---- per-value splitting --------------------------------------------------
+__device__ __forceinline__ int bexp(double x) {
+  return (__double2hiint(x) >> 20) & 0x7FF;
+}
+
+// 53-bit fixed point of x on a row whose largest biased exponent is m, plus
+// the digit bias (see above)
+__device__ __forceinline__ long long to_fixed(double x, int m) {
+  const long long b = __double_as_longlong(x);
+  const int eb = (int)((b >> 52) & 0x7FF);
+  const unsigned long long mant =
+      ((unsigned long long)b & 0xFFFFFFFFFFFFFull) | (eb ? (1ull << 52) : 0ull);
+  const int sh = m - (eb ? eb : 1);
+  unsigned long long X = sh < 64 ? (mant >> sh) : 0ull;
+  long long v = b < 0 ? -(long long)X : (long long)X;
+  return v + (long long)kBias;
+}
+
+// f16 pair of digit j of two biased fixed-point values (low half: a)
+template <int J>
+__device__ __forceinline__ uint32_t digit_pair(long long a, long long b) {
+  const uint32_t wa = J < 4 ? (uint32_t)a : (uint32_t)((unsigned long long)a >> 32);
+  const uint32_t wb = J < 4 ? (uint32_t)b : (uint32_t)((unsigned long long)b >> 32);
+  constexpr uint32_t s = (J % 4) | ((4 + (J % 4)) << 8);
+  const uint32_t u = (__byte_perm(wa, wb, s) & 0x00FF00FFu) | 0x64006400u;  // 1024 + u
+  __half2 h = *reinterpret_cast<const __half2 *>(&u);
+  h = __hsub2(h, __halves2half2(__ushort_as_half(0x6480), __ushort_as_half(0x6480)));  // - 1152
+  return *reinterpret_cast<const uint32_t *>(&h);
+}
+
+__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint2 b) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b.x), "r"(b.y));
+}
+
+// accumulators of one output group: [weight][colgroup][fragment]
+struct Acc {
+  float d[kWeights][2][4];
+  __device__ __forceinline__ void reset() {
+#pragma unroll
+    for (int w = 0; w < kWeights; w++)
+#pragma unroll
+      for (int c = 0; c < 2; c++)
+#pragma unroll
+        for (int r = 0; r < 4; r++) d[w][c][r] = kAccInit;
+  }
+};
+
+// one K block: Y[e][pos] are the biased fixed-point inputs of rows e = 0
+// (g) and 1 (g + 8) at the thread's positions; W points at the block's
+// words in global memory (digit stride 2 * KB * 32; the 18 KB of words stay
+// in L1)
+template <int KB>
+__device__ __forceinline__ void contract(Acc &acc, const long long (&Y)[2][4], const uint2 *W,
+                                         int kb, int lane) {
+  uint32_t A[kDigits][4];
+#define DG_OZ_DIG(J)                                 \
+  A[J][0] = digit_pair<J>(Y[0][0], Y[0][1]);         \
+  A[J][1] = digit_pair<J>(Y[1][0], Y[1][1]);         \
+  A[J][2] = digit_pair<J>(Y[0][2], Y[0][3]);         \
+  A[J][3] = digit_pair<J>(Y[1][2], Y[1][3]);
+  DG_OZ_DIG(0) DG_OZ_DIG(1) DG_OZ_DIG(2) DG_OZ_DIG(3) DG_OZ_DIG(4) DG_OZ_DIG(5) DG_OZ_DIG(6)
+#undef DG_OZ_DIG
+#pragma unroll
+  for (int i = 0; i < kDigits; i++) {
+    const uint2 b0 = __ldg(&W[((i * KB + kb) * 2 + 0) * 32 + lane]);
+    const uint2 b1 = __ldg(&W[((i * KB + kb) * 2 + 1) * 32 + lane]);
+#pragma unroll
+    for (int j = 0; j < kDigits; j++) {
+      if (i + j < kMinPair) continue;
+      const int w = 2 * (kDigits - 1) - i - j;
+      mma16816(acc.d[w][0], A[j], b0);
+      mma16816(acc.d[w][1], A[j], b1);
+    }
+  }
+}
+
+// E * 2^k exactly, |E| < 2^51, k in [-1074, 971]
+__device__ __forceinline__ double scaled_int(long long E, int k) {
+  const long long mb = ((long long)(1075 + k) << 52) | (1ll << 51);
+  return __longlong_as_double(mb + E) - __longlong_as_double(mb);
+}
+
+// output at fragment entry (cg, r): row exponent m (biased, of the row of
+// r >> 1), column exponent M (biased)
+__device__ __forceinline__ double recombine(const Acc &acc, int cg, int r, int m, int M) {
+  int d[kWeights];
+#pragma unroll
+  for (int w = 0; w < kWeights; w++) d[w] = __float_as_int(acc.d[w][cg][r]) - kAccBits;
+  const int ea = d[0] * 256 + d[1], eb = d[2] * 256 + d[3];
+  const int ec = d[4] * 256 + d[5], ed = d[6] * 256 + d[7];
+  const long long E1 = (long long)ea * 65536 + eb, E2 = (long long)ec * 65536 + ed;
+  // value = 2^(m - 1075) 2^(M - 1075) (E1 2^72 + E2 2^40)
+  const int k2 = m + M - 2150 + 40, k1 = k2 + 32;
+  if (m == 0) return 0.0;  // an all-zero (or denormal-only) row
+  if (k2 >= -1074 && k1 <= 971) return scaled_int(E1, k1) + scaled_int(E2, k2);
+  return ldexp((double)E1, k1) + ldexp((double)E2, k2);
+}
+
+// largest biased exponent over a quad's row (all 4 lanes hold the result)
+__device__ __forceinline__ int quad_max(int m) {
+  m = max(m, __shfl_xor_sync(0xffffffffu, m, 1));
+  return max(m, __shfl_xor_sync(0xffffffffu, m, 2));
+}
+
+
+// ---------------------------------------------------------------------------
+// The fused SSP-RK3 element stage (element_body<Eq, P, true>) with the four
+// basis contractions on the tensor cores.  Same inputs, outputs and rules as
+// element_body: volume integral (flattened to the element mean if an area
+// point is non-physical), surface gather (-F on a left face, +F at the
+// mirrored points on a right face), 1/J, the RK combination, the next
+// stage's edge traces and their positivity check.  A block is 4 warps of 16
+// elements; equations without a bed source.  The loops over variables are
+// not unrolled (one copy of each contraction in the code); what crosses
+// them -- area values, metric-folded fluxes, new traces -- is staged per
+// warp in shared memory, each lane in its own column.
+constexpr int kOzThreads = 128, kOzElems = 64;
+
+template <class Eq, int P>
+struct OzShape {
+  static constexpr int N = Eq::N, NP = Tab<P>::NP, NQ = Tab<P>::NQ, N1 = Tab<P>::N1, NF = 3 * N1;
+  static constexpr int PM = npos(NP), PQ = npos(NQ), PF = npos(NF);
+  static constexpr int GH = 2 * PQ * 2 * N;                    // g, h per (point, element, var)
+  static constexpr int UB = N * (PQ > PF ? PQ : PF) * 2;       // area values, then traces
+  static constexpr size_t kSmem = (size_t)4 * (GH + UB) * 32 * sizeof(double);
+};
+
+template <class Eq, int P>
+constexpr size_t oz_smem_bytes() { return OzShape<Eq, P>::kSmem; }
+
+// row exponents (quad-reduced) and biased fixed-point values of two rows
+__device__ __forceinline__ void split_rows(const double (&x)[2][4], int (&m)[2],
+                                           long long (&Y)[2][4]) {
+#pragma unroll
+  for (int e = 0; e < 2; e++) {
+    int mm = 0;
+#pragma unroll
+    for (int p = 0; p < 4; p++) mm = max(mm, bexp(x[e][p]));
+    m[e] = quad_max(mm);
+#pragma unroll
+    for (int p = 0; p < 4; p++) Y[e][p] = to_fixed(x[e][p], max(m[e], 1));
+  }
+}
+
+template <class Eq, int P>
+__global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_constant__ Tab<P> tab,
+                                                           const __grid_constant__ EqP q,
+                                                           const __grid_constant__ ElemArgs a,
+                                                           const Tabs *__restrict__ ozt) {
+  static_assert(!Eq::kBathymetry, "bed source not provided on this path");
+  using S = OzShape<Eq, P>;
+  constexpr int N = S::N, NP = S::NP, NQ = S::NQ, N1 = S::N1, NF = S::NF;
+  constexpr int PM = S::PM, PQ = S::PQ, PF = S::PF;
+  static_assert(NP <= 16 && NQ <= 16 && NF <= 16, "p <= 4");
+  extern __shared__ __align__(16) double smem_d[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, t = lane & 3;
+  double *gh = smem_d + (size_t)warp * (S::GH + S::UB) * 32;
+  double *ub = gh + S::GH * 32;
+  const int K = a.K, Kp = a.Kp;
+  const int e0 = (blockIdx.x * 4 + warp) * 16 + (lane >> 2);
+  const int el[2] = {e0, e0 + 8};
+  const bool live[2] = {el[0] < K, el[1] < K};
+  const int ec[2] = {live[0] ? el[0] : K - 1, live[1] ? el[1] : K - 1};  // loads stay in bounds
+  const double *us = a.us;
+  const uint2 *W = ozt->w;
+  Acc acc;
+
+  // ---- area-point values of every variable -> ub ----
+#pragma unroll 1
+  for (int n = 0; n < N; n++) {
+    double x[2][4];
+#pragma unroll
+    for (int e = 0; e < 2; e++)
+#pragma unroll
+      for (int p = 0; p < 4; p++) {
+        const int idx = p * 4 + t;
+        x[e][p] = (p < PM && idx < NP) ? us[(size_t)(n * NP + idx) * Kp + ec[e]] : 0.0;
+      }
+    int m[2];
+    long long Y[2][4];
+    split_rows(x, m, Y);
+    acc.reset();
+    contract<1>(acc, Y, W + word_off(kEval), 0, lane);
+#pragma unroll
+    for (int p = 0; p < PQ; p++)
+#pragma unroll
+      for (int e = 0; e < 2; e++)
+        ub[((n * PQ + p) * 2 + e) * 32 + lane] =
+            recombine(acc, p >> 1, 2 * e + (p & 1), m[e], ozt->colexp[kEval][slot_of(p, t)]);
+  }
+
+  // ---- positivity of the area values; flatten to the element mean ----
+  bool badv[2] = {false, false};
+#pragma unroll
+  for (int p = 0; p < PQ; p++)
+#pragma unroll
+    for (int e = 0; e < 2; e++) {
+      if (p * 4 + t >= NQ) continue;
+      double u[N];
+#pragma unroll
+      for (int n = 0; n < N; n++) u[n] = ub[((n * PQ + p) * 2 + e) * 32 + lane];
+      badv[e] |= !Eq::physical(q, u);
+    }
+#pragma unroll
+  for (int e = 0; e < 2; e++) {
+    int b = badv[e];
+    b |= __shfl_xor_sync(0xffffffffu, b, 1);
+    b |= __shfl_xor_sync(0xffffffffu, b, 2);
+    badv[e] = b != 0;
+    if (badv[e]) {
+#pragma unroll
+      for (int n = 0; n < N; n++) {
+        const double c0 = us[(size_t)(n * NP) * Kp + ec[e]];
+#pragma unroll
+        for (int p = 0; p < PQ; p++) {
+          const int idx = p * 4 + t;
+          ub[((n * PQ + p) * 2 + e) * 32 + lane] = c0 * tab.B[idx < NQ ? idx : 0][0];
+        }
+      }
+    }
+  }
+
+  // ---- fluxes folded with the metric -> gh ----
+  const double *geo = a.geo;
+  double sc[2];
+  {
+    const double dt = *a.dtp;
+#pragma unroll
+    for (int e = 0; e < 2; e++) sc[e] = a.cc * dt * geo[4 * (size_t)Kp + ec[e]];
+  }
+#pragma unroll
+  for (int e = 0; e < 2; e++) {
+    const double xr = geo[ec[e]], yr = geo[(size_t)Kp + ec[e]];
+    const double xs = geo[2 * (size_t)Kp + ec[e]], ys = geo[3 * (size_t)Kp + ec[e]];
+#pragma unroll
+    for (int p = 0; p < PQ; p++) {
+      double u[N], fx[N], fy[N];
+#pragma unroll
+      for (int n = 0; n < N; n++) u[n] = ub[((n * PQ + p) * 2 + e) * 32 + lane];
+      Eq::flux(q, u, fx, fy);
+      const bool real = p * 4 + t < NQ;
+#pragma unroll
+      for (int n = 0; n < N; n++) {
+        const double gr = fma(fx[n], ys, -fy[n] * xs);
+        const double gs = fma(fy[n], xr, -fx[n] * yr);
+        gh[(((p * 2 + e) * N + n) * 2 + 0) * 32 + lane] = real ? gr : 0.0;
+        gh[(((p * 2 + e) * N + n) * 2 + 1) * 32 + lane] = real ? gs : 0.0;
+      }
+    }
+  }
+
+  // ---- side-flux offsets and signs of the element's edge points ----
+  int foff[PF][2];
+  double fsg[PF][2];
+#pragma unroll
+  for (int p = 0; p < PF; p++)
+#pragma unroll
+    for (int e = 0; e < 2; e++) {
+      const int idx = p * 4 + t;
+      if (idx < NF) {
+        const int f = idx / N1, j = idx % N1;
+        const int sd = a.esd[(size_t)f * Kp + ec[e]];
+        const bool right = sd & 1;
+        foff[p][e] = (sd >> 1) * (N1 * N) + (right ? (N1 - 1 - j) : j) * N;
+        fsg[p][e] = right ? 1.0 : -1.0;
+      } else {
+        foff[p][e] = 0;
+        fsg[p][e] = 0.0;
+      }
+    }
+
+  // ---- per variable: projection, surface, RK combination, traces -> ub ----
+#pragma unroll 1
+  for (int n = 0; n < N; n++) {
+    double R[PM][2];
+    {  // volume: K blocks GR (g values) and GS (h values) over the area points
+      double xg[2][4], xh[2][4];
+#pragma unroll
+      for (int e = 0; e < 2; e++)
+#pragma unroll
+        for (int p = 0; p < 4; p++) {
+          xg[e][p] = p < PQ ? gh[(((p * 2 + e) * N + n) * 2 + 0) * 32 + lane] : 0.0;
+          xh[e][p] = p < PQ ? gh[(((p * 2 + e) * N + n) * 2 + 1) * 32 + lane] : 0.0;
+        }
+      int m[2];
+#pragma unroll
+      for (int e = 0; e < 2; e++) {
+        int mm = 0;
+#pragma unroll
+        for (int p = 0; p < 4; p++) mm = max(mm, max(bexp(xg[e][p]), bexp(xh[e][p])));
+        m[e] = quad_max(mm);
+      }
+      long long Y[2][4];
+      acc.reset();
+#pragma unroll
+      for (int e = 0; e < 2; e++)
+#pragma unroll
+        for (int p = 0; p < 4; p++) Y[e][p] = to_fixed(xg[e][p], max(m[e], 1));
+      contract<2>(acc, Y, W + word_off(kProj), 0, lane);
+#pragma unroll
+      for (int e = 0; e < 2; e++)
+#pragma unroll
+        for (int p = 0; p < 4; p++) Y[e][p] = to_fixed(xh[e][p], max(m[e], 1));
+      contract<2>(acc, Y, W + word_off(kProj), 1, lane);
+#pragma unroll
+      for (int p = 0; p < PM; p++)
+#pragma unroll
+        for (int e = 0; e < 2; e++)
+          R[p][e] = recombine(acc, p >> 1, 2 * e + (p & 1), m[e], ozt->colexp[kProj][slot_of(p, t)]);
+    }
+    {  // surface
+      double xf[2][4];
+#pragma unroll
+      for (int e = 0; e < 2; e++)
+#pragma unroll
+        for (int p = 0; p < 4; p++)
+          xf[e][p] = (p < PF && p * 4 + t < NF)
+                         ? fsg[p < PF ? p : 0][e] * a.Fh[foff[p < PF ? p : 0][e] + n]
+                         : 0.0;
+      int m[2];
+      long long Y[2][4];
+      split_rows(xf, m, Y);
+      acc.reset();
+      contract<1>(acc, Y, W + word_off(kSurf), 0, lane);
+#pragma unroll
+      for (int p = 0; p < PM; p++)
+#pragma unroll
+        for (int e = 0; e < 2; e++)
+          R[p][e] += recombine(acc, p >> 1, 2 * e + (p & 1), m[e], ozt->colexp[kSurf][slot_of(p, t)]);
+    }
+    // RK combination (element_body's epilogue)
+    double cnew[2][4];
+#pragma unroll
+    for (int e = 0; e < 2; e++)
+#pragma unroll
+      for (int p = 0; p < 4; p++) {
+        const int idx = p * 4 + t;
+        cnew[e][p] = 0.0;
+        if (p < PM && idx < NP) {
+          const size_t o = (size_t)(n * NP + idx) * Kp + ec[e];
+          const double cin = (badv[e] && idx > 0) ? 0.0 : us[o];
+          double v = fma(sc[e], R[p < PM ? p : 0][e], a.cb * cin);
+          if (a.ca != 0.0) v = fma(a.ca, a.un[o], v);
+          if (live[e]) {
+            a.out[o] = v;
+            if (badv[e] && idx > 0 && a.us != a.out) a.us[o] = 0.0;
+          }
+          cnew[e][p] = v;
+        }
+      }
+    // next-stage edge traces
+    int m[2];
+    long long Y[2][4];
+    split_rows(cnew, m, Y);
+    acc.reset();
+    contract<1>(acc, Y, W + word_off(kTrace), 0, lane);
+#pragma unroll
+    for (int p = 0; p < PF; p++)
+#pragma unroll
+      for (int e = 0; e < 2; e++)
+        ub[((n * PF + p) * 2 + e) * 32 + lane] =
+            recombine(acc, p >> 1, 2 * e + (p & 1), m[e], ozt->colexp[kTrace][slot_of(p, t)]);
+  }
+
+  // lane t = 0 wrote each element's mode 0 to out; the flatten below reads it
+  __syncwarp();
+  // ---- positivity of the new traces; write them ----
+  bool badt[2] = {false, false};
+#pragma unroll
+  for (int p = 0; p < PF; p++)
+#pragma unroll
+    for (int e = 0; e < 2; e++) {
+      if (p * 4 + t >= NF) continue;
+      double u[N];
+#pragma unroll
+      for (int n = 0; n < N; n++) u[n] = ub[((n * PF + p) * 2 + e) * 32 + lane];
+      badt[e] |= !Eq::physical(q, u);
+    }
+#pragma unroll
+  for (int e = 0; e < 2; e++) {
+    int b = badt[e] && a.check;
+    b |= __shfl_xor_sync(0xffffffffu, b, 1);
+    b |= __shfl_xor_sync(0xffffffffu, b, 2);
+    badt[e] = b != 0;
+  }
+#pragma unroll
+  for (int e = 0; e < 2; e++) {
+    if (!live[e]) continue;
+    double *Te = a.T + (size_t)el[e] * (NF * N);
+    double c0[N];
+    if (badt[e]) {  // the element mean, as written to out above
+#pragma unroll
+      for (int n = 0; n < N; n++) c0[n] = a.out[(size_t)(n * NP) * Kp + el[e]];
+    }
+#pragma unroll
+    for (int p = 0; p < PF; p++) {
+      const int idx = p * 4 + t;
+      if (idx >= NF) continue;
+      const int f = idx / N1, j = idx % N1;
+#pragma unroll
+      for (int n = 0; n < N; n++)
+        Te[idx * N + n] = badt[e] ? c0[n] * tab.E[f][j][0] : ub[((n * PF + p) * 2 + e) * 32 + lane];
+    }
+  }
+  if (badt[0] || badt[1]) {
+#pragma unroll
+    for (int e = 0; e < 2; e++) {
+      if (!live[e] || !badt[e]) continue;
+#pragma unroll
+      for (int n = 0; n < N; n++)
+#pragma unroll
+        for (int p = 0; p < PM; p++) {
+          const int idx = p * 4 + t;
+          if (idx >= 1 && idx < NP) a.out[(size_t)(n * NP + idx) * Kp + el[e]] = 0.0;
+        }
+    }
+  }
+}
+
+// Edge traces of a state with the tensor-core trace contraction (trace_body's
+// rules: a non-physical trace flattens the element -- higher modes to zero,
+// traces to the mean).  Bit for bit the traces k_element_oz writes for the
+// same coefficients, so a run that starts from a stored state continues
+// exactly as an uninterrupted one.
+template <class Eq, int P>
+__global__ void __launch_bounds__(kOzThreads) k_trace_oz(const __grid_constant__ Tab<P> tab,
+                                                         const __grid_constant__ EqP q,
+                                                         double *u, double *__restrict__ T, int K,
+                                                         int Kp, const Tabs *__restrict__ ozt) {
+  using S = OzShape<Eq, P>;
+  constexpr int N = S::N, NP = S::NP, N1 = S::N1, NF = S::NF, PM = S::PM, PF = S::PF;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, t = lane & 3;
+  const int e0 = (blockIdx.x * 4 + warp) * 16 + (lane >> 2);
+  const int el[2] = {e0, e0 + 8};
+  const bool live[2] = {el[0] < K, el[1] < K};
+  const int ec[2] = {live[0] ? el[0] : K - 1, live[1] ? el[1] : K - 1};
+  Acc acc;
+  double Tv[N][PF][2];
+#pragma unroll
+  for (int n = 0; n < N; n++) {
+    double x[2][4];
+#pragma unroll
+    for (int e = 0; e < 2; e++)
+#pragma unroll
+      for (int p = 0; p < 4; p++) {
+        const int idx = p * 4 + t;
+        x[e][p] = (p < PM && idx < NP) ? u[(size_t)(n * NP + idx) * Kp + ec[e]] : 0.0;
+      }
+    int m[2];
+    long long Y[2][4];
+    split_rows(x, m, Y);
+    acc.reset();
+    contract<1>(acc, Y, ozt->w + word_off(kTrace), 0, lane);
+#pragma unroll
+    for (int p = 0; p < PF; p++)
+#pragma unroll
+      for (int e = 0; e < 2; e++)
+        Tv[n][p][e] = recombine(acc, p >> 1, 2 * e + (p & 1), m[e], ozt->colexp[kTrace][slot_of(p, t)]);
+  }
+  bool bad[2] = {false, false};
+#pragma unroll
+  for (int p = 0; p < PF; p++)
+#pragma unroll
+    for (int e = 0; e < 2; e++) {
+      if (p * 4 + t >= NF) continue;
+      double v[N];
+#pragma unroll
+      for (int n = 0; n < N; n++) v[n] = Tv[n][p][e];
+      bad[e] |= !Eq::physical(q, v);
+    }
+#pragma unroll
+  for (int e = 0; e < 2; e++) {
+    int b = bad[e];
+    b |= __shfl_xor_sync(0xffffffffu, b, 1);
+    b |= __shfl_xor_sync(0xffffffffu, b, 2);
+    bad[e] = b != 0;
+  }
+#pragma unroll
+  for (int e = 0; e < 2; e++) {
+    if (!live[e]) continue;
+    double *Te = T + (size_t)el[e] * (NF * N);
+    double c0[N];
+    if (bad[e]) {
+#pragma unroll
+      for (int n = 0; n < N; n++) c0[n] = u[(size_t)(n * NP) * Kp + el[e]];
+    }
+#pragma unroll
+    for (int p = 0; p < PF; p++) {
+      const int idx = p * 4 + t;
+      if (idx >= NF) continue;
+      const int f = idx / N1, j = idx % N1;
+#pragma unroll
+      for (int n = 0; n < N; n++) Te[idx * N + n] = bad[e] ? c0[n] * tab.E[f][j][0] : Tv[n][p][e];
+    }
+  }
+  if (bad[0] || bad[1]) {
+#pragma unroll
+    for (int e = 0; e < 2; e++) {
+      if (!live[e] || !bad[e]) continue;
+#pragma unroll
+      for (int n = 0; n < N; n++)
+#pragma unroll
+        for (int p = 0; p < PM; p++) {
+          const int idx = p * 4 + t;
+          if (idx >= 1 && idx < NP) u[(size_t)(n * NP + idx) * Kp + el[e]] = 0.0;
+        }
+    }
+  }
+}
+
+// host: the f16 digit words and column exponents of the four tables
+template <int P>
+void build_tabs(const Tab<P> &tb, Tabs *out);
+
+}  // namespace oz
+}  // namespace dg

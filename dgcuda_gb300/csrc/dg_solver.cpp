@@ -49,6 +49,12 @@ struct dg_solver {
   double *bathy = nullptr;        // bed modes (shallow water), internal order
   double *lin_tv = nullptr, *lin_f0 = nullptr, *lin_f1 = nullptr;  // adjoint work
   bool has_inout_bc = false;      // a side with an inflow or outflow code
+  void *oz = nullptr;             // tensor-core tables (Euler, p = 1..4)
+  bool tensor = true;             // use them in the fused element stage
+  // T holds the traces of U as the last fused SSP-RK3 stage left them (and U
+  // is already limited): the next dg_step continues without recomputing
+  // them, so a run split over several calls is the uninterrupted run
+  bool tr_valid = false;
   std::vector<double> mesh_v;     // vertices per element, .pmsh order (bed projection)
   dg::DevScalars *ds = nullptr;
   double dmin = 0;
@@ -236,6 +242,24 @@ void drop_graphs(dg_solver *s) {
   s->graph_launches.clear();
 }
 
+// (re)builds the tensor-core tables from the current basis tables and
+// points the fused element stage at them (or back at the FP64 kernel)
+dg_status oz_refresh(dg_solver *s) {
+  s->ctx.oz = nullptr;
+  if (s->eq != DG_EULER || s->p < 1 || s->p > 4) return DG_OK;
+  std::vector<char> img(dg::oz_tabs_bytes());
+  if (!dg::oz_build_tabs(s->p, s->tabimg.data(), img.data()))
+    return fail(DG_UNSUPPORTED, "no tensor-core tables for this order");
+  if (!s->oz) {
+    dg_status st = dalloc(s, reinterpret_cast<char **>(&s->oz), img.size());
+    if (st != DG_OK) return st;
+    CK(dg::oz_prepare_euler(s->p));
+  }
+  CK(cudaMemcpy(s->oz, img.data(), img.size(), cudaMemcpyHostToDevice));
+  if (s->tensor) s->ctx.oz = s->oz;
+  return DG_OK;
+}
+
 dg_status get_graph(dg_solver *s, int scheme, cudaGraphExec_t *out) {
   int key = scheme * 2 + (s->prm.limiter ? 1 : 0);
   auto it = s->graphs.find(key);
@@ -303,10 +327,14 @@ dg_status run_steps(dg_solver *s, int nsteps, int scheme, double fixed_dt, doubl
   h.endtime = endtime;
   dg_status st = set_scalar(s, 0, &h, sizeof h);
   if (st != DG_OK) return st;
-  // the reference limits once before its step loop (time_integrator.cu:178-184)
-  limit(s, s->U);
-  // SSP-RK3 stages find their input traces in T (fused_stage)
-  if (scheme == DG_SSP_RK3) run(s, K_TRACE, [&] { s->ops->trace(s->ctx, s->U); });
+  const bool resume = scheme == DG_SSP_RK3 && s->tr_valid;
+  s->tr_valid = false;
+  if (!resume) {
+    // the reference limits once before its step loop (time_integrator.cu:178-184)
+    limit(s, s->U);
+    // SSP-RK3 stages find their input traces in T (fused_stage)
+    if (scheme == DG_SSP_RK3) run(s, K_TRACE, [&] { s->ops->trace(s->ctx, s->U); });
+  }
   cudaGraphExec_t g = nullptr;
   if (!s->profiling) {
     st = get_graph(s, scheme, &g);
@@ -350,6 +378,7 @@ dg_status run_steps(dg_solver *s, int nsteps, int scheme, double fixed_dt, doubl
   *t = h.t;
   if (taken) *taken = (int)h.steps;
   if (h.status == 4) return fail(DG_NAN, "time step is NaN or not positive (non-finite state?)");
+  s->tr_valid = scheme == DG_SSP_RK3;
   return DG_OK;
 }
 
@@ -553,6 +582,8 @@ extern "C" dg_status dg_solver_create(const dg_mesh *mesh, dg_equation eq, int p
   c.T = s->T;
   c.Fh = s->Fh;
   c.ds = s->ds;
+  dg_status ozs = oz_refresh(s);
+  if (ozs != DG_OK) return bail(ozs);
   *out = s;
   return DG_OK;
 }
@@ -591,6 +622,7 @@ extern "C" dg_status dg_solver_set_tables(dg_solver *s, int n_q, int n_1, const 
   if (!s || !basis || !grad_x || !grad_y || !side || !vertex || !w || !r1 || !r2 || !r_oned ||
       !w_oned)
     return fail(DG_BAD_ARG, "null argument");
+  s->tr_valid = false;
   if (n_q != dg::nq_of(s->p) || n_1 != s->p + 1)
     return fail(DG_BAD_ARG, "table sizes do not match the order p");
   dg_order_tables t{};
@@ -619,11 +651,16 @@ extern "C" dg_status dg_solver_set_tables(dg_solver *s, int n_q, int n_1, const 
   s->tables = t;
   dg::build_tab(s->p, s->tables, s->tabimg.data());
   drop_graphs(s);
+  {
+    dg_status ozs = oz_refresh(s);
+    if (ozs != DG_OK) return ozs;
+  }
   return DG_OK;
 }
 
 extern "C" dg_status dg_init(dg_solver *s) {
   if (!s) return fail(DG_BAD_ARG, "null solver");
+  s->tr_valid = false;
   CK(cudaSetDevice(s->device));
   run(s, K_RK, [&] { s->ops->init(s->ctx, s->U); });
   collect_profile(s);
@@ -632,6 +669,7 @@ extern "C" dg_status dg_init(dg_solver *s) {
 
 extern "C" dg_status dg_set_state(dg_solver *s, const double *C) {
   if (!s || !C) return fail(DG_BAD_ARG, "null argument");
+  s->tr_valid = false;
   CK(cudaSetDevice(s->device));
   size_t n = (size_t)s->N * s->np * s->K;
   CK(cudaMemcpyAsync(s->ubuf, C, n * sizeof(double), cudaMemcpyHostToDevice, s->st));
@@ -650,6 +688,7 @@ extern "C" dg_status dg_get_state(dg_solver *s, double *C) {
 
 extern "C" dg_status dg_set_state_device(dg_solver *s, const double *C) {
   if (!s || !C) return fail(DG_BAD_ARG, "null argument");
+  s->tr_valid = false;
   CK(cudaSetDevice(s->device));
   dg::launch_permute_in(s->st, C, s->U, s->m.perm, s->N * s->np, s->K, s->m.Kp);
   return sync_check(s);
@@ -664,6 +703,7 @@ extern "C" dg_status dg_get_state_device(dg_solver *s, double *C) {
 
 extern "C" dg_status dg_rhs(dg_solver *s, double t, const double *C, double *dCdt) {
   if (!s || !C || !dCdt) return fail(DG_BAD_ARG, "null argument");
+  s->tr_valid = false;
   CK(cudaSetDevice(s->device));
   size_t n = (size_t)s->N * s->np * s->K;
   double *in = s->W, *out = nullptr;
@@ -683,6 +723,7 @@ extern "C" dg_status dg_rhs(dg_solver *s, double t, const double *C, double *dCd
 
 extern "C" dg_status dg_limit(dg_solver *s) {
   if (!s) return fail(DG_BAD_ARG, "null solver");
+  s->tr_valid = false;
   CK(cudaSetDevice(s->device));
   if (s->np >= 3) run(s, K_LIMIT, [&] { s->ops->limit(s->ctx, s->U); });
   collect_profile(s);
@@ -753,6 +794,7 @@ extern "C" dg_status dg_l2_error(dg_solver *s, double t, double *err) {
 // ---- shallow-water bed ---------------------------------------------------
 extern "C" dg_status dg_set_bathymetry(dg_solver *s, const double *b) {
   if (!s) return fail(DG_BAD_ARG, "null solver");
+  s->tr_valid = false;
   if (s->eq != DG_SHALLOW_WATER) return fail(DG_UNSUPPORTED, "bathymetry needs shallow water");
   CK(cudaSetDevice(s->device));
   if (!b) {
@@ -787,6 +829,7 @@ extern "C" dg_status dg_get_bathymetry(dg_solver *s, double *b) {
 
 extern "C" dg_status dg_bathymetry_project(dg_solver *s, int kind, const double *prm) {
   if (!s) return fail(DG_BAD_ARG, "null solver");
+  s->tr_valid = false;
   if (kind == DG_BED_FLAT) return dg_set_bathymetry(s, nullptr);
   if (!prm) return fail(DG_BAD_ARG, "null parameters");
   if (kind != DG_BED_SINE && kind != DG_BED_LINEAR) return fail(DG_BAD_ARG, "unknown bed kind");
@@ -833,6 +876,7 @@ const int kTuneBlocks[] = {64, 128, 256};
 
 extern "C" dg_status dg_autotune(dg_solver *s, int *block) {
   if (!s) return fail(DG_BAD_ARG, "null solver");
+  s->tr_valid = false;
   CK(cudaSetDevice(s->device));
   double *save = nullptr;
   CK(cudaMalloc(&save, s->ndof_p * sizeof(double)));
@@ -849,6 +893,7 @@ extern "C" dg_status dg_autotune(dg_solver *s, int *block) {
       st = time_steps(s->st, [&] { return run_steps(s, 3, DG_SSP_RK3, 0.0, 0.0, &t, nullptr); },
                       &ms);
     cudaMemcpyAsync(s->U, save, s->ndof_p * sizeof(double), cudaMemcpyDeviceToDevice, s->st);
+    s->tr_valid = false;  // T belongs to the advanced state
     if (st != DG_OK) {
       cudaFree(save);
       return st;
@@ -1078,6 +1123,7 @@ extern "C" dg_status dg_batch_create(int n, dg_solver *const *members, dg_batch 
 
 extern "C" dg_status dg_batch_step(dg_batch *b, int nsteps, double *t) {
   if (!b || nsteps < 0) return fail(DG_BAD_ARG, "bad batch step arguments");
+  for (dg_solver *s : b->m) s->tr_valid = false;
   return batch_run(b, nsteps, t);
 }
 
@@ -1193,6 +1239,7 @@ dg_status lin_check(dg_solver *s) {
 extern "C" dg_status dg_rhs_tl(dg_solver *s, double t, const double *C, const double *dC,
                                const double *db, double *dL) {
   if (!s || !C || !dC || !dL) return fail(DG_BAD_ARG, "null argument");
+  s->tr_valid = false;
   dg_status st = lin_check(s);
   if (st != DG_OK) return st;
   CK(cudaSetDevice(s->device));
@@ -1224,6 +1271,7 @@ extern "C" dg_status dg_rhs_tl(dg_solver *s, double t, const double *C, const do
 extern "C" dg_status dg_rhs_adjoint(dg_solver *s, double t, const double *C, const double *Lbar,
                                     double *Cbar, double *bbar) {
   if (!s || !C || !Lbar || !Cbar) return fail(DG_BAD_ARG, "null argument");
+  s->tr_valid = false;
   dg_status st = lin_check(s);
   if (st != DG_OK) return st;
   CK(cudaSetDevice(s->device));
@@ -1376,6 +1424,7 @@ extern "C" dg_status dg_adjoint_forward(dg_adjoint *a, int nsteps, double dt, in
   if (!a || nsteps <= 0 || !(dt > 0) || every <= 0 || ckpt <= 0)
     return fail(DG_BAD_ARG, "bad forward arguments");
   dg_solver *s = a->s;
+  s->tr_valid = false;
   CK(cudaSetDevice(s->device));
   dg_status st;
   const int nck = (nsteps + ckpt - 1) / ckpt, nsamp = nsteps / every;
@@ -1437,6 +1486,7 @@ extern "C" dg_status dg_adjoint_backward(dg_adjoint *a, const double *sbar, doub
                                          double *grad_b) {
   if (!a || !sbar || a->cks.empty()) return fail(DG_BAD_ARG, "no forward run to differentiate");
   dg_solver *s = a->s;
+  s->tr_valid = false;
   CK(cudaSetDevice(s->device));
   dg_status st;
   LinBufs lb;
@@ -1511,6 +1561,7 @@ extern "C" dg_status dg_adjoint_tangent(dg_adjoint *a, const double *du0, const 
                                         double *dsamples) {
   if (!a || a->cks.empty()) return fail(DG_BAD_ARG, "no forward run to differentiate");
   dg_solver *s = a->s;
+  s->tr_valid = false;
   CK(cudaSetDevice(s->device));
   dg_status st;
   LinBufs lb;
@@ -1705,5 +1756,25 @@ extern "C" dg_status dg_load_checkpoint(dg_solver *s, const char *path, double *
   if (s->eq == DG_SHALLOW_WATER && (st = dg_set_bathymetry(s, hdr[5] ? b.data() : nullptr)) != DG_OK)
     return st;
   if (t) *t = tt;
+  return DG_OK;
+}
+
+// the fused element stage's basis contractions on the tensor cores (exact
+// slices, FP64 accuracy) or in FP64 FMAs; Euler p = 1..4 have the former
+extern "C" dg_status dg_set_tensor_contractions(dg_solver *s, int on) {
+  if (!s) return fail(DG_BAD_ARG, "null solver");
+  s->tr_valid = false;
+  if (on && !s->oz) return fail(DG_UNSUPPORTED, "tensor-core contractions are for Euler, p = 1..4");
+  CK(cudaSetDevice(s->device));
+  CK(cudaStreamSynchronize(s->st));
+  s->tensor = on != 0;
+  s->ctx.oz = s->tensor ? s->oz : nullptr;
+  drop_graphs(s);
+  return DG_OK;
+}
+
+extern "C" dg_status dg_get_tensor_contractions(dg_solver *s, int *on) {
+  if (!s || !on) return fail(DG_BAD_ARG, "null argument");
+  *on = s->ctx.oz != nullptr;
   return DG_OK;
 }

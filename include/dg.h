@@ -180,6 +180,15 @@ dg_status dg_eval_vertices(dg_solver *s, int var, double *uv);
 #define DG_VIEW_ERROR 2
 dg_status dg_eval_vertices_view(dg_solver *s, int var, int view, double t, double *uv);
 
+/* The fused SSP-RK3 element stage computes its basis contractions (area
+ * values, volume and surface projections, next-stage traces) either with
+ * FP64 FMAs or on the tensor cores as exact integer slices (Ozaki-style
+ * FP64 emulation; per-output error of the order of an FP64 dot product's
+ * rounding).  The tensor path exists for Euler at p = 1..4 and is on by
+ * default there; DG_UNSUPPORTED elsewhere.  No reference counterpart. */
+dg_status dg_set_tensor_contractions(dg_solver *s, int on);
+dg_status dg_get_tensor_contractions(dg_solver *s, int *on);
+
 /* binary checkpoint / restart (no reference counterpart: the reference's
  * output is vertex values only).  The file holds the equation, order,
  * sizes, the time t, the state in .pmsh order, the shallow-water bed when

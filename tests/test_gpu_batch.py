@@ -40,6 +40,9 @@ def test_batched_euler_with_limiter_bitwise(dglib):
             s = dg.Solver(m, dg.EULER, p, problem="euler_riemann4", limiter=1, cfl=0.2)
             s.init_conditions()
             lst.append(s)
+    # the batched kernels contract in FP64: compare with solvers doing the same
+    for s in singles:
+        s.tensor_contractions = False
     dg.Batch(members).step(8)
     for a, b in zip(members, singles):
         b.step(8, dg.SSP_RK3, 0.0)

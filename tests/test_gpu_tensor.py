@@ -1,0 +1,98 @@
+"""The fused element stage with its basis contractions on the tensor cores
+(exact integer slices, Euler p = 1..4) against the FP64-FMA kernel and the
+oracle: same steps, results equal to FP64 rounding."""
+import numpy as np
+import pytest
+
+from conftest import relerr
+
+pytestmark = pytest.mark.gpu
+VTX = (5.0, 5.0, 5.0, 1.0, 1.0, 10.0)
+
+
+def vortex(dg, p, n=24):
+    mesh = dg.Mesh.square(n, n, box=(0, 10, 0, 10), jitter=0.15, seed=2)
+    s = dg.Solver(mesh, dg.EULER, p, problem="euler_vortex", prm=VTX, cfl=0.2)
+    s.init_conditions()
+    return mesh, s
+
+
+@pytest.mark.parametrize("p", [1, 2, 3, 4])
+def test_tensor_path_matches_fp64_path(dglib, p):
+    dg = dglib
+    _, a = vortex(dg, p)
+    _, b = vortex(dg, p)
+    assert a.tensor_contractions
+    b.tensor_contractions = False
+    assert not b.tensor_contractions
+    ta = a.step(20, dg.SSP_RK3, 0.0)
+    tb = b.step(20, dg.SSP_RK3, 0.0)
+    assert abs(ta - tb) <= 1e-14 * tb
+    assert relerr(a.get_state(), b.get_state(), 4) <= 1e-12
+
+
+@pytest.mark.parametrize("p", [2, 3])
+def test_tensor_path_matches_oracle(dglib, oracle_mod, p):
+    dg = dglib
+    mesh, s = vortex(dg, p, n=12)
+    c0 = s.get_state()
+    o = oracle_mod.Oracle.from_mesh(mesh, dg.EULER, p, oracle_mod.prm_vec(extra=VTX),
+                                    dg.PROBLEMS["euler_vortex"])
+    t = s.step(10, dg.SSP_RK3, 0.0)
+    c, to, _ = o.step(c0, 10, 0, 0, 0.2)
+    assert abs(t - to) <= 1e-12 * to
+    assert relerr(s.get_state(), c, 4) <= 1e-10
+
+
+def test_tensor_path_limiter_and_transmissive(dglib):
+    dg = dglib
+    mesh = dg.Mesh.square(48, 48, jitter=0.1, seed=3, bc=(-4, -4, -4, -4))
+    kw = dict(problem="euler_riemann4", limiter=1, cfl=0.2)
+    a = dg.Solver(mesh, dg.EULER, 3, **kw)
+    b = dg.Solver(mesh, dg.EULER, 3, **kw)
+    b.tensor_contractions = False
+    for s in (a, b):
+        s.init_conditions()
+    ta, tb = a.step(10, dg.SSP_RK3, 0.0), b.step(10, dg.SSP_RK3, 0.0)
+    assert abs(ta - tb) <= 1e-13 * tb
+    assert relerr(a.get_state(), b.get_state(), 4) <= 1e-10
+
+
+def test_tensor_path_unsupported_elsewhere(dglib):
+    dg = dglib
+    mesh = dg.Mesh.square(4, 4, jitter=0.1, seed=1)
+    s = dg.Solver(mesh, dg.ADVECTION, 2, problem="adv_sine")
+    assert not s.tensor_contractions
+    with pytest.raises(dg.DGError):
+        s.tensor_contractions = True
+    s.tensor_contractions = False
+
+
+@pytest.mark.parametrize("limiter", [0, 1])
+def test_split_runs_equal_one_run(dglib, limiter):
+    """dg_step(10) twice gives the bits of dg_step(20): the second call
+    continues from the traces the first one left."""
+    dg = dglib
+    mesh = dg.Mesh.square(24, 24, jitter=0.1, seed=3, bc=(-4, -4, -4, -4))
+    kw = dict(problem="euler_riemann4", limiter=limiter, cfl=0.2)
+    a, b = dg.Solver(mesh, dg.EULER, 3, **kw), dg.Solver(mesh, dg.EULER, 3, **kw)
+    for s in (a, b):
+        s.init_conditions()
+    t = a.step(10, dg.SSP_RK3, 0.0)
+    ta = a.step(10, dg.SSP_RK3, t)
+    tb = b.step(20, dg.SSP_RK3, 0.0)
+    assert ta == tb and np.array_equal(a.get_state(), b.get_state())
+
+
+def test_restart_from_state_equals_one_run(dglib):
+    """A fresh solver given the state after 10 steps continues bit for bit:
+    the start-of-run traces use the same tensor contraction as the stage."""
+    dg = dglib
+    _, a = vortex(dg, 3)
+    _, b = vortex(dg, 3)
+    t = a.step(10, dg.SSP_RK3, 0.0)
+    c = a.get_state()
+    ta = a.step(10, dg.SSP_RK3, t)
+    b.set_state(c)
+    tb = b.step(10, dg.SSP_RK3, t)
+    assert ta == tb and np.array_equal(a.get_state(), b.get_state())
