@@ -68,27 +68,25 @@ int slot(int item) { return slot_of(item / 4, item % 4); }
 template <int P>
 void build_tabs(const Tab<P> &tb, Tabs *out) {
   constexpr int NP = Tab<P>::NP, NQ = Tab<P>::NQ, N1 = Tab<P>::N1;
-  static double T[2][16][16];
+  static double T[3][16][16];
   std::memset(out, 0, sizeof *out);
   // EVAL: u(q) = sum_i c_i B[q][i]
   std::memset(T, 0, sizeof T);
   for (int q = 0; q < NQ; q++)
     for (int i = 0; i < NP; i++) T[0][slot(i)][slot(q)] = tb.B[q][i];
   split_table(T, 1, out->w + word_off(kEval), out->colexp[kEval]);
-  // PROJ: r_i = sum_q GR[q][i] g_q + GS[q][i] h_q
+  // PROJ: r_i = sum_q GR[q][i] g_q + GS[q][i] h_q + sum_fj E[f][j][i] F_fj
   std::memset(T, 0, sizeof T);
   for (int q = 0; q < NQ; q++)
     for (int i = 0; i < NP; i++) {
       T[0][slot(q)][slot(i)] = tb.GR[q][i];
       T[1][slot(q)][slot(i)] = tb.GS[q][i];
     }
-  split_table(T, 2, out->w + word_off(kProj), out->colexp[kProj]);
-  // SURF: r_i = sum_fj E[f][j][i] F_fj ; TRACE: u_fj = sum_i E[f][j][i] c_i
-  std::memset(T, 0, sizeof T);
   for (int f = 0; f < 3; f++)
     for (int j = 0; j < N1; j++)
-      for (int i = 0; i < NP; i++) T[0][slot(f * N1 + j)][slot(i)] = tb.E[f][j][i];
-  split_table(T, 1, out->w + word_off(kSurf), out->colexp[kSurf]);
+      for (int i = 0; i < NP; i++) T[2][slot(f * N1 + j)][slot(i)] = tb.E[f][j][i];
+  split_table(T, 3, out->w + word_off(kProj), out->colexp[kProj]);
+  // TRACE: u_fj = sum_i E[f][j][i] c_i
   std::memset(T, 0, sizeof T);
   for (int f = 0; f < 3; f++)
     for (int j = 0; j < N1; j++)

@@ -20,13 +20,12 @@
 //  * every digit pair (i, j) with i + j >= 5 is one f16 MMA with f32
 //    accumulation; pairs of equal weight 256^(i+j) share an accumulator.  A
 //    product is at most 2^14, a weight class has at most 7 pairs, a group
-//    accumulates at most 32 real K slots (p <= 4), so every partial sum is an
-//    integer below 7 * 32 * 2^14 < 2^22 in magnitude: the accumulator starts at 1.5 * 2^23, where
+//    accumulates at most 36 real K slots, so every partial sum is an
+//    integer below 7 * 36 * 2^14 < 2^22 in magnitude: the accumulator starts at 1.5 * 2^23, where
 //    fp32 holds every integer of the window exactly, and the integer is read
 //    back from its bits;
-//  * the 8 weight sums are combined in 64-bit integers and turned into one
-//    double with two exact conversions (a power-of-two bias added to the
-//    integer bits, the bias subtracted in FP64) and one rounding.
+//  * the 8 weight sums are combined into one 128-bit integer and rounded
+//    to the nearest double with integer instructions (no FP64 work).
 //  The pairs left out (i + j < 5) and the truncation of the inputs bound the
 //  error of each output by about 2^-52 max|x| max|t| times the slot count,
 //  the order of an FP64 dot product's own rounding.
@@ -58,19 +57,20 @@ constexpr unsigned long long kBias = 0x80808080808080ull;
 constexpr float kAccInit = 12582912.0f;     // 1.5 * 2^23
 constexpr int kAccBits = 0x4B400000;        // its bit pattern
 
-// tables: EVAL (K = modes, N = area points), PROJ (2 K blocks: GR, GS over
-// area points; N = modes), SURF (K = edge points, N = modes), TRACE (K =
-// modes, N = edge points).  Words are the B fragments of each lane:
-// word[digit][kblock][colgroup][lane] = {k 2t..2t+1, k 2t+8..2t+9} of column
-// colgroup * 8 + g, as f16 pairs.
-enum { kEval = 0, kProj = 1, kSurf = 2, kTrace = 3 };
+// tables: EVAL (K = modes, N = area points), PROJ (3 K blocks: GR and GS
+// over the area points, E over the edge points; N = modes; one exponent per
+// column across the three), TRACE (K = modes, N = edge points).  Words are
+// the B fragments of each lane: word[digit][kblock][colgroup][lane] =
+// {k 2t..2t+1, k 2t+8..2t+9} of column colgroup * 8 + g, as f16 pairs.
+enum { kEval = 0, kProj = 1, kTrace = 2 };
 // word offset of each table: 7 digits x 2 column groups x 32 lanes per K
-// block, K blocks 1, 2, 1, 1
-__host__ __device__ constexpr int word_off(int tab) { return 7 * 2 * 32 * (tab <= 1 ? tab : tab + 1); }
+// block, K blocks 1, 3, 1
+__host__ __device__ constexpr int word_off(int tab) { return 7 * 2 * 32 * (tab == 0 ? 0 : tab == 1 ? 1 : 4); }
 constexpr int kWords = 7 * 5 * 2 * 32;      // 2240 uint2
 struct Tabs {
   uint2 w[kWords];
-  int colexp[4][16];                         // biased exponent of each table column
+  int colexp[3][16];                         // biased exponent of each table column
+  int pad[16];
 };
 
 // position p of lane quad index t -> slot (0..15); item index of (p, t)
@@ -157,26 +157,60 @@ __device__ __forceinline__ void contract(Acc &acc, const long long (&Y)[2][4], c
   }
 }
 
-// E * 2^k exactly, |E| < 2^51, k in [-1074, 971]
-__device__ __forceinline__ double scaled_int(long long E, int k) {
-  const long long mb = ((long long)(1075 + k) << 52) | (1ll << 51);
-  return __longlong_as_double(mb + E) - __longlong_as_double(mb);
-}
-
 // output at fragment entry (cg, r): row exponent m (biased, of the row of
-// r >> 1), column exponent M (biased)
+// r >> 1), column exponent M (biased).  The value is S 2^k with the exact
+// integer S = sum_w d_w 256^(7 - w) (below 2^79 in magnitude) and k = m + M
+// - 2110; it is rounded to the nearest double (ties to even) with integer
+// instructions only: S as a 128-bit two's complement pair, its magnitude
+// normalised by a leading-zero count, 53 bits kept, the rest as round and
+// sticky bits.
 __device__ __forceinline__ double recombine(const Acc &acc, int cg, int r, int m, int M) {
+  if (m == 0) return 0.0;  // an all-zero (or denormal-only) row
   int d[kWeights];
 #pragma unroll
   for (int w = 0; w < kWeights; w++) d[w] = __float_as_int(acc.d[w][cg][r]) - kAccBits;
-  const int ea = d[0] * 256 + d[1], eb = d[2] * 256 + d[3];
-  const int ec = d[4] * 256 + d[5], ed = d[6] * 256 + d[7];
-  const long long E1 = (long long)ea * 65536 + eb, E2 = (long long)ec * 65536 + ed;
-  // value = 2^(m - 1075) 2^(M - 1075) (E1 2^72 + E2 2^40)
-  const int k2 = m + M - 2150 + 40, k1 = k2 + 32;
-  if (m == 0) return 0.0;  // an all-zero (or denormal-only) row
-  if (k2 >= -1074 && k1 <= 971) return scaled_int(E1, k1) + scaled_int(E2, k2);
-  return ldexp((double)E1, k1) + ldexp((double)E2, k2);
+  const long long Sh = (long long)d[0] * 65536 + (long long)d[1] * 256 + d[2];  // |Sh| < 2^39
+  const long long Sl = (long long)d[3] * 4294967296ll + (long long)d[4] * 16777216 +
+                       (long long)d[5] * 65536 + (long long)d[6] * 256 + d[7];  // |Sl| < 2^55
+  // S = Sh 2^40 + Sl as (hi, lo)
+  unsigned long long lo = (unsigned long long)Sh << 40;
+  long long hi = Sh >> 24;
+  const unsigned long long l2 = lo + (unsigned long long)Sl;
+  hi += (Sl >> 63) + (l2 < lo ? 1 : 0);
+  lo = l2;
+  const bool neg = hi < 0;
+  if (neg) {
+    lo = ~lo + 1;
+    hi = ~hi + (lo == 0 ? 1 : 0);
+  }
+  if (hi == 0 && lo == 0) return 0.0;
+  const unsigned long long uh = (unsigned long long)hi;
+  int lz;
+  unsigned long long top, rest;
+  if (uh) {
+    lz = __clzll(uh);
+    top = lz ? (uh << lz) | (lo >> (64 - lz)) : uh;
+    rest = lz ? lo << lz : lo;
+  } else {
+    lz = 64 + __clzll(lo);
+    top = lo << (lz - 64);
+    rest = 0;
+  }
+  unsigned long long mant = top >> 11;  // 53 bits; its unit is 2^(75 - lz) in S
+  const unsigned long long rbit = (top >> 10) & 1, sticky = ((top & 0x3FF) | rest) != 0;
+  mant += rbit & (sticky | (mant & 1));
+  int ex = 75 - lz;
+  if (mant >> 53) {
+    mant >>= 1;
+    ex++;
+  }
+  const int k = m + M - 2110, e = ex + 52 + k + 1023;
+  if (e >= 1 && e <= 2046)
+    return __longlong_as_double((long long)((neg ? 1ull << 63 : 0ull) | ((unsigned long long)e << 52) |
+                                            (mant & 0xFFFFFFFFFFFFFull)));
+  // out of the normal range: scale in two steps (never on physical data)
+  const double v = ldexp((double)(long long)mant, ex);
+  return ldexp(neg ? -v : v, k);
 }
 
 // largest biased exponent over a quad's row (all 4 lanes hold the result)
@@ -356,22 +390,33 @@ __global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_const
 #pragma unroll 1
   for (int n = 0; n < N; n++) {
     double R[PM][2];
-    {  // volume: K blocks GR (g values) and GS (h values) over the area points
-      double xg[2][4], xh[2][4];
+    {  // volume (K blocks GR, GS over the area points) and surface (K block E
+       // over the edge points) into one accumulator when the exactness
+       // bound allows it (7 * 36 * 2^14 < 2^22), else two
+      double xg[2][4], xh[2][4], xf[2][4];
 #pragma unroll
       for (int e = 0; e < 2; e++)
 #pragma unroll
         for (int p = 0; p < 4; p++) {
           xg[e][p] = p < PQ ? gh[(((p * 2 + e) * N + n) * 2 + 0) * 32 + lane] : 0.0;
           xh[e][p] = p < PQ ? gh[(((p * 2 + e) * N + n) * 2 + 1) * 32 + lane] : 0.0;
+          xf[e][p] = (p < PF && p * 4 + t < NF)
+                         ? fsg[p < PF ? p : 0][e] * a.Fh[foff[p < PF ? p : 0][e] + n]
+                         : 0.0;
         }
-      int m[2];
+      constexpr bool kMerge = 2 * NQ + NF <= 36;
+      int m[2], mf[2];
 #pragma unroll
       for (int e = 0; e < 2; e++) {
-        int mm = 0;
+        int mv = 0, ms = 0;
 #pragma unroll
-        for (int p = 0; p < 4; p++) mm = max(mm, max(bexp(xg[e][p]), bexp(xh[e][p])));
-        m[e] = quad_max(mm);
+        for (int p = 0; p < 4; p++) {
+          mv = max(mv, max(bexp(xg[e][p]), bexp(xh[e][p])));
+          ms = max(ms, bexp(xf[e][p]));
+        }
+        if (kMerge) mv = max(mv, ms);
+        m[e] = quad_max(mv);
+        mf[e] = kMerge ? m[e] : quad_max(ms);
       }
       long long Y[2][4];
       acc.reset();
@@ -379,37 +424,32 @@ __global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_const
       for (int e = 0; e < 2; e++)
 #pragma unroll
         for (int p = 0; p < 4; p++) Y[e][p] = to_fixed(xg[e][p], max(m[e], 1));
-      contract<2>(acc, Y, W + word_off(kProj), 0, lane);
+      contract<3>(acc, Y, W + word_off(kProj), 0, lane);
 #pragma unroll
       for (int e = 0; e < 2; e++)
 #pragma unroll
         for (int p = 0; p < 4; p++) Y[e][p] = to_fixed(xh[e][p], max(m[e], 1));
-      contract<2>(acc, Y, W + word_off(kProj), 1, lane);
+      contract<3>(acc, Y, W + word_off(kProj), 1, lane);
+      if (!kMerge) {
 #pragma unroll
-      for (int p = 0; p < PM; p++)
+        for (int p = 0; p < PM; p++)
 #pragma unroll
-        for (int e = 0; e < 2; e++)
-          R[p][e] = recombine(acc, p >> 1, 2 * e + (p & 1), m[e], ozt->colexp[kProj][slot_of(p, t)]);
-    }
-    {  // surface
-      double xf[2][4];
+          for (int e = 0; e < 2; e++)
+            R[p][e] = recombine(acc, p >> 1, 2 * e + (p & 1), m[e], ozt->colexp[kProj][slot_of(p, t)]);
+        acc.reset();
+      }
 #pragma unroll
       for (int e = 0; e < 2; e++)
 #pragma unroll
-        for (int p = 0; p < 4; p++)
-          xf[e][p] = (p < PF && p * 4 + t < NF)
-                         ? fsg[p < PF ? p : 0][e] * a.Fh[foff[p < PF ? p : 0][e] + n]
-                         : 0.0;
-      int m[2];
-      long long Y[2][4];
-      split_rows(xf, m, Y);
-      acc.reset();
-      contract<1>(acc, Y, W + word_off(kSurf), 0, lane);
+        for (int p = 0; p < 4; p++) Y[e][p] = to_fixed(xf[e][p], max(mf[e], 1));
+      contract<3>(acc, Y, W + word_off(kProj), 2, lane);
 #pragma unroll
       for (int p = 0; p < PM; p++)
 #pragma unroll
-        for (int e = 0; e < 2; e++)
-          R[p][e] += recombine(acc, p >> 1, 2 * e + (p & 1), m[e], ozt->colexp[kSurf][slot_of(p, t)]);
+        for (int e = 0; e < 2; e++) {
+          const double v = recombine(acc, p >> 1, 2 * e + (p & 1), mf[e], ozt->colexp[kProj][slot_of(p, t)]);
+          R[p][e] = kMerge ? v : R[p][e] + v;
+        }
     }
     // RK combination (element_body's epilogue)
     double cnew[2][4];
