@@ -102,6 +102,7 @@ def _declare(L):
         "dg_profile_reset": (C.c_int, [C.c_void_p]),
         "dg_kernel_launches": (C.c_longlong, [C.c_void_p]),
         "dg_measure_fp64_peak": (C.c_int, [C.c_int, _dp]),
+        "dg_probe_reciprocal": (C.c_int, [C.c_int, C.c_int, _dp, _dp, _dp]),
         "dg_eval_vertices": (C.c_int, [C.c_void_p, C.c_int, _dp]),
         "dg_eval_vertices_view": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, _dp]),
         "dg_save_checkpoint": (C.c_int, [C.c_void_p, C.c_char_p, C.c_double]),
@@ -215,6 +216,16 @@ class Adjoint:
 
     def __del__(self):
         self.close()
+
+
+def probe_reciprocal(x, device=0):
+    """(rcp(x), 1/x) computed on the device: the flux kernels' reciprocal and
+    IEEE division."""
+    L = load_library()
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    r, q = np.empty_like(x), np.empty_like(x)
+    _check(L.dg_probe_reciprocal(device, x.size, _dptr(x), _dptr(r), _dptr(q)))
+    return r, q
 
 
 def measure_fp64_peak(device=0):
@@ -409,7 +420,7 @@ class Solver:
     @property
     def tensor_contractions(self):
         """True when the fused element stage runs its contractions on the
-        tensor cores (Euler, p = 1..4, default on)."""
+        tensor cores (Euler, p = 1..4; on by default from p = 2)."""
         v = np.zeros(1, dtype=np.int32)
         _check(self._L.dg_get_tensor_contractions(self._h, _iptr(v)))
         return bool(v[0])

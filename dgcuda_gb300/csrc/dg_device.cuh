@@ -52,6 +52,25 @@ DG_HD double mul_rn(double a, double b) {
 #endif
 }
 
+// 1/x for the flux evaluations, by Newton-Raphson iteration (r <- r + r (1 -
+// x r), quadratic convergence) from the approximate reciprocal of the PTX
+// instruction rcp.approx.ftz.f64: two steps take its ~20 correct bits past
+// the 53 of a double; the result is within 1 ulp of 1/x for normal x
+// (checked against IEEE division by dg_probe_reciprocal).  It costs four
+// FMAs where an IEEE division costs about twice that.
+DG_HD double rcp(double x) {
+#ifdef __CUDA_ARCH__
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  double e = fma(-x, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-x, r, 1.0);
+  return fma(r, e, r);
+#else
+  return 1.0 / x;
+#endif
+}
+
 // --------------------------------------------------------------------------
 // problem plugins: exact / initial / inflow state (U0, U_exact, U_inflow)
 // --------------------------------------------------------------------------
@@ -170,7 +189,7 @@ struct Euler {  // euler/euler.cu
     return !(2.0 * U[0] * U[3] < fma(U[1], U[1], U[2] * U[2]));
   }
   DG_HD static void flux(const EqP &q, const double *U, double *fx, double *fy) {
-    double ir = 1.0 / U[0];
+    double ir = rcp(U[0]);
     double u = U[1] * ir, v = U[2] * ir;
     // p is reused as an addend: round it explicitly (never fused into an FMA)
     double p = mul_rn(q.gamma - 1., fma(-0.5, fma(U[1], u, U[2] * v), U[3]));
@@ -189,7 +208,7 @@ struct Euler {  // euler/euler.cu
                             double *F) {
     // every multiply-add is an explicit fma so the rounding does not depend
     // on how the compiler contracts the expression in a given kernel
-    double irl = 1.0 / UL[0], irr = 1.0 / UR[0];
+    double irl = rcp(UL[0]), irr = rcp(UR[0]);
     double ul = UL[1] * irl, vl = UL[2] * irl, ur = UR[1] * irr, vr = UR[2] * irr;
     double pl = mul_rn(q.gamma - 1., fma(-0.5, fma(UL[1], ul, UL[2] * vl), UL[3]));
     double pr = mul_rn(q.gamma - 1., fma(-0.5, fma(UR[1], ur, UR[2] * vr), UR[3]));
@@ -237,7 +256,7 @@ struct ShallowWater {  // shallowwater/shallowwater.cu (g is a parameter here)
   static constexpr bool kBathymetry = true;  // optional bed b(x, y): source -g h grad b
   DG_HD static bool physical(const EqP &, const double *U) { return U[0] >= 0.; }
   DG_HD static void flux(const EqP &q, const double *U, double *fx, double *fy) {
-    double ih = 1.0 / U[0];
+    double ih = rcp(U[0]);
     double u = U[1] * ih, v = U[2] * ih, hp = 0.5 * q.g * U[0] * U[0];
     fx[0] = U[1];
     fx[1] = fma(U[1], u, hp);
@@ -248,7 +267,7 @@ struct ShallowWater {  // shallowwater/shallowwater.cu (g is a parameter here)
   }
   DG_HD static void riemann(const EqP &q, const double *UL, const double *UR, double nx, double ny,
                             double *F) {  // shallowwater.cu:118-185
-    double ihl = 1.0 / UL[0], ihr = 1.0 / UR[0];
+    double ihl = rcp(UL[0]), ihr = rcp(UR[0]);
     double snl = fma(nx, UL[1], ny * UL[2]) * ihl, snr = fma(nx, UR[1], ny * UR[2]) * ihr;
     double cl = sqrt(UL[0] * q.g), cr = sqrt(UR[0] * q.g);
     double lam = fmax(fabs(snl) + cl, fabs(snr) + cr);

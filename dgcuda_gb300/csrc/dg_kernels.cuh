@@ -381,9 +381,12 @@ __global__ void __launch_bounds__(kMaxBlock) k_limit(const __grid_constant__ Tab
         up = fmax(up, d);
         dn = fmax(dn, -d);
       }
+    // a quotient >= 1 leaves alpha as it is, and a / b >= 1 exactly when
+    // a >= b > 0 (IEEE division is monotonic): divide only when it limits
     double alpha = 1.0;
-    if (up > 0.0) alpha = fmin(alpha, (Uc - Umin) / up);
-    if (dn > 0.0) alpha = fmin(alpha, (Umax - Uc) / dn);
+    const double lo = Uc - Umin, hi = Umax - Uc;
+    if (up > lo) alpha = fmin(alpha, lo / up);
+    if (dn > hi) alpha = fmin(alpha, hi / dn);
     if (alpha < 0.0) alpha = 0.0;
     if (alpha < 1.0) {
       double *w = u + (size_t)(n * NP) * Kp;
@@ -446,9 +449,12 @@ __device__ __forceinline__ void limit_tr_body(const Tab<P> &tab, const EqP &q, d
     }
     const double up = fmax(0.0, from_order_key(kmax) - Uc);
     const double dn = fmax(0.0, Uc - from_order_key(kmin));
+    // a quotient >= 1 leaves alpha as it is, and a / b >= 1 exactly when
+    // a >= b > 0 (IEEE division is monotonic): divide only when it limits
     double alpha = 1.0;
-    if (up > 0.0) alpha = fmin(alpha, (Uc - Umin) / up);
-    if (dn > 0.0) alpha = fmin(alpha, (Umax - Uc) / dn);
+    const double lo = Uc - Umin, hi = Umax - Uc;
+    if (up > lo) alpha = fmin(alpha, lo / up);
+    if (dn > hi) alpha = fmin(alpha, hi / dn);
     if (alpha < 0.0) alpha = 0.0;
     if (alpha < 1.0) {
       const double c1 = row[(size_t)1 * Kp + e] * alpha, c2 = row[(size_t)2 * Kp + e] * alpha;

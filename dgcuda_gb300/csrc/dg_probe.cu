@@ -4,6 +4,7 @@
 
 #include <string>
 
+#include "dg_device.cuh"
 #include "dg_internal.h"
 
 namespace {
@@ -20,7 +21,35 @@ __global__ void k_fma64(double *out, int iters, double a, double b) {
   for (int k = 0; k < 8; k++) s += x[k];
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
+__global__ void k_reciprocal(const double *x, double *r, double *q, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    r[i] = dg::rcp(x[i]);
+    q[i] = 1.0 / x[i];
+  }
+}
 }  // namespace
+
+// the flux kernels' reciprocal (dg::rcp) and IEEE division on the device for
+// n host values: r[i] = rcp(x[i]), q[i] = 1 / x[i]
+extern "C" dg_status dg_probe_reciprocal(int device, int n, const double *x, double *r,
+                                         double *q) {
+  if (n < 0 || (n && (!x || !r || !q))) return dg::fail(DG_BAD_ARG, "bad arguments");
+  if (!n) return DG_OK;
+  if (cudaSetDevice(device) != cudaSuccess) return dg::fail(DG_CUDA_ERROR, "cudaSetDevice");
+  double *d = nullptr;
+  const size_t b = sizeof(double) * (size_t)n;
+  if (cudaMalloc(&d, 3 * b) != cudaSuccess) return dg::fail(DG_CUDA_ERROR, "cudaMalloc");
+  cudaError_t e = cudaMemcpy(d, x, b, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    k_reciprocal<<<(n + 255) / 256, 256>>>(d, d + n, d + 2 * (size_t)n, n);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(r, d + n, b, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(q, d + 2 * (size_t)n, b, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  return e == cudaSuccess ? DG_OK : dg::fail(DG_CUDA_ERROR, cudaGetErrorString(e));
+}
 
 extern "C" dg_status dg_measure_fp64_peak(int device, double *tflops) {
   if (!tflops) return dg::fail(DG_BAD_ARG, "null argument");

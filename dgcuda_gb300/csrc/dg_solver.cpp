@@ -247,6 +247,9 @@ void drop_graphs(dg_solver *s) {
 dg_status oz_refresh(dg_solver *s) {
   s->ctx.oz = nullptr;
   if (s->eq != DG_EULER || s->p < 1 || s->p > 4) return DG_OK;
+  // at p = 1 (3 modes, 3 area points) the FP64 kernel is the faster one:
+  // the tensor path is built but off until asked for
+  if (!s->oz) s->tensor = s->p >= 2;
   std::vector<char> img(dg::oz_tabs_bytes());
   if (!dg::oz_build_tabs(s->p, s->tabimg.data(), img.data()))
     return fail(DG_UNSUPPORTED, "no tensor-core tables for this order");

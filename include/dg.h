@@ -185,7 +185,8 @@ dg_status dg_eval_vertices_view(dg_solver *s, int var, int view, double t, doubl
  * FP64 FMAs or on the tensor cores as exact integer slices (Ozaki-style
  * FP64 emulation; per-output error of the order of an FP64 dot product's
  * rounding).  The tensor path exists for Euler at p = 1..4 and is on by
- * default there; DG_UNSUPPORTED elsewhere.  No reference counterpart. */
+ * default at p = 2..4 (at p = 1 the FP64 kernel is faster); DG_UNSUPPORTED
+ * elsewhere.  No reference counterpart. */
 dg_status dg_set_tensor_contractions(dg_solver *s, int on);
 dg_status dg_get_tensor_contractions(dg_solver *s, int *on);
 
@@ -287,6 +288,10 @@ dg_status dg_rhs_device_noalloc(dg_solver *s, double t, const double *C_device,
 /* FP64 FMA throughput of `device` in TFLOP/s (the binding roof of the DG
  * kernels on GB300), timed with CUDA events; no reference counterpart */
 dg_status dg_measure_fp64_peak(int device, double *tflops);
+/* the reciprocal the flux kernels use (Newton-Raphson from the hardware's
+ * approximate reciprocal) and IEEE division, on the device, for n host
+ * values: r[i] = rcp(x[i]), q[i] = 1 / x[i] (a check of the former) */
+dg_status dg_probe_reciprocal(int device, int n, const double *x, double *r, double *q);
 
 #ifdef __cplusplus
 }

@@ -22,7 +22,8 @@ def test_tensor_path_matches_fp64_path(dglib, p):
     dg = dglib
     _, a = vortex(dg, p)
     _, b = vortex(dg, p)
-    assert a.tensor_contractions
+    assert a.tensor_contractions == (p >= 2)  # default: on from p = 2
+    a.tensor_contractions = True
     b.tensor_contractions = False
     assert not b.tensor_contractions
     ta = a.step(20, dg.SSP_RK3, 0.0)
@@ -96,3 +97,16 @@ def test_restart_from_state_equals_one_run(dglib):
     b.set_state(c)
     tb = b.step(10, dg.SSP_RK3, t)
     assert ta == tb and np.array_equal(a.get_state(), b.get_state())
+
+
+def test_flux_reciprocal_within_one_ulp(dglib):
+    """The flux kernels' Newton-Raphson reciprocal against IEEE division on
+    the GPU, over 12 decades and both signs."""
+    dg = dglib
+    rng = np.random.default_rng(7)
+    x = 10.0 ** rng.uniform(-6, 6, 200000) * rng.choice([-1.0, 1.0], 200000)
+    x = np.concatenate([x, [1.0, 2.0, 0.5, 3.0, 1.4, 1e-3, 7.0e5]])
+    r, q = dg.probe_reciprocal(x)
+    ulp = np.abs(r - q) / np.spacing(np.abs(q))
+    assert ulp.max() <= 1.0
+    assert np.array_equal(q, 1.0 / x)
