@@ -164,8 +164,11 @@ struct Advection {  // advection/advection.cu
     fy[0] = q.ay * U[0];
   }
   // upwind flux (riemann_solver_upwind, advection.cu:94-116)
-  DG_HD static void riemann(const EqP &q, const double *UL, const double *UR, double nx, double ny,
-                            double *F) {
+  // riemann_raw(..) * kRawScale is the numerical flux; face kernels fold the
+  // (exact, power-of-two) scale into their own edge-length factor
+  static constexpr double kRawScale = 1.0;
+  DG_HD static void riemann_raw(const EqP &q, const double *UL, const double *UR, double nx,
+                                double ny, double *F) {
     double an = fma(nx, q.ax, ny * q.ay);
     F[0] = an > 0 ? an * UL[0] : an * UR[0];
   }
@@ -204,8 +207,9 @@ struct Euler {  // euler/euler.cu
     fy[3] = H * v;
   }
   // local Lax-Friedrichs (euler.cu:170-237)
-  DG_HD static void riemann(const EqP &q, const double *UL, const double *UR, double nx, double ny,
-                            double *F) {
+  static constexpr double kRawScale = 0.5;  // LLF: F = 0.5 [ ... ]
+  DG_HD static void riemann_raw(const EqP &q, const double *UL, const double *UR, double nx,
+                                double ny, double *F) {
     // every multiply-add is an explicit fma so the rounding does not depend
     // on how the compiler contracts the expression in a given kernel
     double irl = rcp(UL[0]), irr = rcp(UR[0]);
@@ -215,10 +219,10 @@ struct Euler {  // euler/euler.cu
     double snl = fma(nx, ul, ny * vl), snr = fma(nx, ur, ny * vr);
     double cl = sqrt(q.gamma * pl * irl), cr = sqrt(q.gamma * pr * irr);
     double lam = fmax(fabs(snl) + cl, fabs(snr) + cr);
-    F[0] = 0.5 * fma(lam, UL[0] - UR[0], fma(UL[0], snl, UR[0] * snr));
-    F[1] = 0.5 * fma(lam, UL[1] - UR[1], fma(UL[1], snl, fma(pl, nx, fma(UR[1], snr, pr * nx))));
-    F[2] = 0.5 * fma(lam, UL[2] - UR[2], fma(UL[2], snl, fma(pl, ny, fma(UR[2], snr, pr * ny))));
-    F[3] = 0.5 * fma(lam, UL[3] - UR[3], fma(UL[3] + pl, snl, (UR[3] + pr) * snr));
+    F[0] = fma(lam, UL[0] - UR[0], fma(UL[0], snl, UR[0] * snr));
+    F[1] = fma(lam, UL[1] - UR[1], fma(UL[1], snl, fma(pl, nx, fma(UR[1], snr, pr * nx))));
+    F[2] = fma(lam, UL[2] - UR[2], fma(UL[2], snl, fma(pl, ny, fma(UR[2], snr, pr * ny))));
+    F[3] = fma(lam, UL[3] - UR[3], fma(UL[3] + pl, snl, (UR[3] + pr) * snr));
   }
   DG_HD static double mean_speed(const EqP &q, const double *U) {  // euler.cu:248-277
     const double m2 = fma(U[1], U[1], U[2] * U[2]);
@@ -265,16 +269,17 @@ struct ShallowWater {  // shallowwater/shallowwater.cu (g is a parameter here)
     fy[1] = U[1] * v;
     fy[2] = fma(U[2], v, hp);
   }
-  DG_HD static void riemann(const EqP &q, const double *UL, const double *UR, double nx, double ny,
-                            double *F) {  // shallowwater.cu:118-185
+  static constexpr double kRawScale = 0.5;  // LLF: F = 0.5 [ ... ]
+  DG_HD static void riemann_raw(const EqP &q, const double *UL, const double *UR, double nx,
+                                double ny, double *F) {  // shallowwater.cu:118-185
     double ihl = rcp(UL[0]), ihr = rcp(UR[0]);
     double snl = fma(nx, UL[1], ny * UL[2]) * ihl, snr = fma(nx, UR[1], ny * UR[2]) * ihr;
     double cl = sqrt(UL[0] * q.g), cr = sqrt(UR[0] * q.g);
     double lam = fmax(fabs(snl) + cl, fabs(snr) + cr);
     double pl = 0.5 * q.g * UL[0] * UL[0], pr = 0.5 * q.g * UR[0] * UR[0];
-    F[0] = 0.5 * fma(lam, UL[0] - UR[0], fma(UL[0], snl, UR[0] * snr));
-    F[1] = 0.5 * fma(lam, UL[1] - UR[1], fma(UL[1], snl, fma(pl, nx, fma(UR[1], snr, pr * nx))));
-    F[2] = 0.5 * fma(lam, UL[2] - UR[2], fma(UL[2], snl, fma(pl, ny, fma(UR[2], snr, pr * ny))));
+    F[0] = fma(lam, UL[0] - UR[0], fma(UL[0], snl, UR[0] * snr));
+    F[1] = fma(lam, UL[1] - UR[1], fma(UL[1], snl, fma(pl, nx, fma(UR[1], snr, pr * nx))));
+    F[2] = fma(lam, UL[2] - UR[2], fma(UL[2], snl, fma(pl, ny, fma(UR[2], snr, pr * ny))));
   }
   DG_HD static double mean_speed(const EqP &q, const double *U) {  // shallowwater.cu:196-224
     double c = sqrt(U[0] * q.g);
@@ -304,13 +309,14 @@ struct Maxwell {  // maxwells/maxwells.cu, U = (Hx, Hy, Ez)
     fy[1] = 0.;
     fy[2] = -ieps * U[0];
   }
-  DG_HD static void riemann(const EqP &q, const double *UL, const double *UR, double nx, double ny,
-                            double *F) {  // maxwells.cu:93-163, LLF with lambda = 1/sqrt(eps mu)
+  static constexpr double kRawScale = 0.5;  // LLF: F = 0.5 [ ... ]
+  DG_HD static void riemann_raw(const EqP &q, const double *UL, const double *UR, double nx,
+                                double ny, double *F) {  // maxwells.cu:93-163, LLF with lambda = 1/sqrt(eps mu)
     double imu = 1. / q.mu, ieps = 1. / q.eps, lam = fabs(1. / sqrt(q.eps * q.mu));
     double ez = UL[2] + UR[2], hx = UL[0] + UR[0], hy = UL[1] + UR[1];
-    F[0] = 0.5 * fma(lam, UL[0] - UR[0], -imu * ez * ny);
-    F[1] = 0.5 * fma(lam, UL[1] - UR[1], imu * ez * nx);
-    F[2] = 0.5 * fma(lam, UL[2] - UR[2], ieps * fma(hy, nx, -hx * ny));
+    F[0] = fma(lam, UL[0] - UR[0], -imu * ez * ny);
+    F[1] = fma(lam, UL[1] - UR[1], imu * ez * nx);
+    F[2] = fma(lam, UL[2] - UR[2], ieps * fma(hy, nx, -hx * ny));
   }
   DG_HD static double mean_speed(const EqP &q, const double *) { return fabs(1. / sqrt(q.eps * q.mu)); }
   DG_HD static void reflect(const EqP &, const double *UL, double *UR, double, double, double nx,

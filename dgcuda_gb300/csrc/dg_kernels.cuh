@@ -127,8 +127,8 @@ __device__ __forceinline__ void face_body(const Tab<P> &tab, const EqP &q, const
         UL[n] = TL[j * N + n];
         UR[n] = TR[(N1 - 1 - j) * N + n];
       }
-      Eq::riemann(q, UL, UR, nx, ny, Fn);
-      const double sc = hl * tab.w1[j];
+      Eq::riemann_raw(q, UL, UR, nx, ny, Fn);
+      const double sc = hl * tab.w1[j] * Eq::kRawScale;  // exact: a power of two
 #pragma unroll
       for (int n = 0; n < N; n++) F[j * N + n] = Fn[n] * sc;
     }
@@ -143,8 +143,8 @@ __device__ __forceinline__ void face_body(const Tab<P> &tab, const EqP &q, const
       for (int n = 0; n < N; n++) UL[n] = TL[j * N + n];
       const double r = 0.5 + 0.5 * tab.t1[j];
       ghost_state<Eq>(q, sd.y, UL, UR, fma(r, xb - xa, xa), fma(r, yb - ya, ya), t, nx, ny);
-      Eq::riemann(q, UL, UR, nx, ny, Fn);
-      const double sc = hl * tab.w1[j];
+      Eq::riemann_raw(q, UL, UR, nx, ny, Fn);
+      const double sc = hl * tab.w1[j] * Eq::kRawScale;  // exact: a power of two
 #pragma unroll
       for (int n = 0; n < N; n++) F[j * N + n] = Fn[n] * sc;
     }
@@ -462,11 +462,13 @@ __device__ __forceinline__ void limit_tr_body(const Tab<P> &tab, const EqP &q, d
       row[(size_t)2 * Kp + e] = c2;
 #pragma unroll
       for (int i = 3; i < NP; i++) row[(size_t)i * Kp + e] = 0.0;
+      // basis function 0 is constant: c0 phi_0 is one product for every point
+      const double a0 = c0[n] * tab.E[0][0][0];
 #pragma unroll
       for (int f = 0; f < 3; f++)
 #pragma unroll
         for (int j = 0; j < N1; j++) {
-          double a = c0[n] * tab.E[f][j][0];
+          double a = a0;
           a = fma(c1, tab.E[f][j][1], a);
           a = fma(c2, tab.E[f][j][2], a);
           Te[(f * N1 + j) * N + n] = a;
@@ -485,10 +487,11 @@ __device__ __forceinline__ void limit_tr_body(const Tab<P> &tab, const EqP &q, d
     for (int n = 0; n < N; n++) {
 #pragma unroll
       for (int i = 1; i < NP; i++) u[(size_t)(n * NP + i) * Kp + e] = 0.0;
+      const double a0 = c0[n] * tab.E[0][0][0];
 #pragma unroll
       for (int f = 0; f < 3; f++)
 #pragma unroll
-        for (int j = 0; j < N1; j++) Te[(f * N1 + j) * N + n] = c0[n] * tab.E[f][j][0];
+        for (int j = 0; j < N1; j++) Te[(f * N1 + j) * N + n] = a0;
     }
   }
 }
