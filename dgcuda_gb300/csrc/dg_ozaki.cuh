@@ -115,6 +115,16 @@ __device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], 
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b.x), "r"(b.y));
 }
 
+// the same for a K block that uses only K slots 0..7 (thread positions 0 and
+// 1): the first halves of the k16 fragments
+__device__ __forceinline__ void mma1688(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t b) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5}, {%6}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a0), "r"(a1), "r"(b));
+}
+
 // accumulators of one output group: [weight][colgroup][fragment]
 struct Acc {
   float d[kWeights][2][4];
@@ -132,7 +142,10 @@ struct Acc {
 // (g) and 1 (g + 8) at the thread's positions; W points at the block's
 // words in global memory (digit stride 2 * KB * 32; the 18 KB of words stay
 // in L1)
-template <int KB>
+// (NCG: how many of the two column groups of 8 outputs are needed; K8: the
+// block's inputs fill only positions 0 and 1.  At p <= 2 the area points and
+// modes fill only the first column group and K slots 0..7)
+template <int KB, int NCG = 2, bool K8 = false>
 __device__ __forceinline__ void contract(Acc &acc, const long long (&Y)[2][4], const uint2 *W,
                                          int kb, int lane) {
   uint32_t A[kDigits][4];
@@ -146,13 +159,18 @@ __device__ __forceinline__ void contract(Acc &acc, const long long (&Y)[2][4], c
 #pragma unroll
   for (int i = 0; i < kDigits; i++) {
     const uint2 b0 = __ldg(&W[((i * KB + kb) * 2 + 0) * 32 + lane]);
-    const uint2 b1 = __ldg(&W[((i * KB + kb) * 2 + 1) * 32 + lane]);
+    const uint2 b1 = NCG > 1 ? __ldg(&W[((i * KB + kb) * 2 + 1) * 32 + lane]) : b0;
 #pragma unroll
     for (int j = 0; j < kDigits; j++) {
       if (i + j < kMinPair) continue;
       const int w = 2 * (kDigits - 1) - i - j;
-      mma16816(acc.d[w][0], A[j], b0);
-      mma16816(acc.d[w][1], A[j], b1);
+      if (K8) {
+        mma1688(acc.d[w][0], A[j][0], A[j][1], b0.x);
+        if (NCG > 1) mma1688(acc.d[w][1], A[j][0], A[j][1], b1.x);
+      } else {
+        mma16816(acc.d[w][0], A[j], b0);
+        if (NCG > 1) mma16816(acc.d[w][1], A[j], b1);
+      }
     }
   }
 }
@@ -297,7 +315,7 @@ __global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_const
     long long Y[2][4];
     split_rows(x, m, Y);
     acc.reset();
-    contract<1>(acc, Y, W + word_off(kEval), 0, lane);
+    contract<1, (PQ + 1) / 2, (PM <= 2)>(acc, Y, W + word_off(kEval), 0, lane);
 #pragma unroll
     for (int p = 0; p < PQ; p++)
 #pragma unroll
@@ -424,12 +442,12 @@ __global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_const
       for (int e = 0; e < 2; e++)
 #pragma unroll
         for (int p = 0; p < 4; p++) Y[e][p] = to_fixed(xg[e][p], max(m[e], 1));
-      contract<3>(acc, Y, W + word_off(kProj), 0, lane);
+      contract<3, (PM + 1) / 2, (PQ <= 2)>(acc, Y, W + word_off(kProj), 0, lane);
 #pragma unroll
       for (int e = 0; e < 2; e++)
 #pragma unroll
         for (int p = 0; p < 4; p++) Y[e][p] = to_fixed(xh[e][p], max(m[e], 1));
-      contract<3>(acc, Y, W + word_off(kProj), 1, lane);
+      contract<3, (PM + 1) / 2, (PQ <= 2)>(acc, Y, W + word_off(kProj), 1, lane);
       if (!kMerge) {
 #pragma unroll
         for (int p = 0; p < PM; p++)
@@ -442,7 +460,7 @@ __global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_const
       for (int e = 0; e < 2; e++)
 #pragma unroll
         for (int p = 0; p < 4; p++) Y[e][p] = to_fixed(xf[e][p], max(mf[e], 1));
-      contract<3>(acc, Y, W + word_off(kProj), 2, lane);
+      contract<3, (PM + 1) / 2, (PF <= 2)>(acc, Y, W + word_off(kProj), 2, lane);
 #pragma unroll
       for (int p = 0; p < PM; p++)
 #pragma unroll
@@ -476,7 +494,7 @@ __global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_const
     long long Y[2][4];
     split_rows(cnew, m, Y);
     acc.reset();
-    contract<1>(acc, Y, W + word_off(kTrace), 0, lane);
+    contract<1, (PF + 1) / 2, (PM <= 2)>(acc, Y, W + word_off(kTrace), 0, lane);
 #pragma unroll
     for (int p = 0; p < PF; p++)
 #pragma unroll
@@ -573,7 +591,7 @@ __global__ void __launch_bounds__(kOzThreads) k_trace_oz(const __grid_constant__
     long long Y[2][4];
     split_rows(x, m, Y);
     acc.reset();
-    contract<1>(acc, Y, ozt->w + word_off(kTrace), 0, lane);
+    contract<1, (PF + 1) / 2, (PM <= 2)>(acc, Y, ozt->w + word_off(kTrace), 0, lane);
 #pragma unroll
     for (int p = 0; p < PF; p++)
 #pragma unroll
