@@ -464,15 +464,23 @@ __device__ __forceinline__ void limit_tr_body(const Tab<P> &tab, const EqP &q, d
       for (int i = 3; i < NP; i++) row[(size_t)i * Kp + e] = 0.0;
       // basis function 0 is constant: c0 phi_0 is one product for every point
       const double a0 = c0[n] * tab.E[0][0][0];
+      if (alpha == 0.0 && a0 != 0.0) {
+        // c1 = c2 = +-0 add nothing to a nonzero a0: the traces are a0 (the
+        // common case: a uniform region, where the limiter removes
+        // rounding-sized higher modes)
 #pragma unroll
-      for (int f = 0; f < 3; f++)
+        for (int k = 0; k < 3 * N1; k++) Te[k * N + n] = a0;
+      } else {
 #pragma unroll
-        for (int j = 0; j < N1; j++) {
-          double a = a0;
-          a = fma(c1, tab.E[f][j][1], a);
-          a = fma(c2, tab.E[f][j][2], a);
-          Te[(f * N1 + j) * N + n] = a;
-        }
+        for (int f = 0; f < 3; f++)
+#pragma unroll
+          for (int j = 0; j < N1; j++) {
+            double a = a0;
+            a = fma(c1, tab.E[f][j][1], a);
+            a = fma(c2, tab.E[f][j][2], a);
+            Te[(f * N1 + j) * N + n] = a;
+          }
+      }
     }
   }
 #pragma unroll

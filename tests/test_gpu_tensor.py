@@ -4,7 +4,7 @@ oracle: same steps, results equal to FP64 rounding."""
 import numpy as np
 import pytest
 
-from conftest import relerr
+from conftest import ref_tables, relerr, split_tables
 
 pytestmark = pytest.mark.gpu
 VTX = (5.0, 5.0, 5.0, 1.0, 1.0, 10.0)
@@ -32,7 +32,7 @@ def test_tensor_path_matches_fp64_path(dglib, p):
     assert relerr(a.get_state(), b.get_state(), 4) <= 1e-12
 
 
-@pytest.mark.parametrize("p", [2, 3])
+@pytest.mark.parametrize("p", [2, 3, 4])
 def test_tensor_path_matches_oracle(dglib, oracle_mod, p):
     dg = dglib
     mesh, s = vortex(dg, p, n=12)
@@ -110,3 +110,43 @@ def test_flux_reciprocal_within_one_ulp(dglib):
     ulp = np.abs(r - q) / np.spacing(np.abs(q))
     assert ulp.max() <= 1.0
     assert np.array_equal(q, 1.0 / x)
+
+
+def _oracle_run(dg, oracle_mod, mesh, p, prm, pb, c0, nsteps, lim, cfl, tables=None):
+    o = oracle_mod.Oracle.from_mesh(mesh, dg.EULER, p, oracle_mod.prm_vec(extra=prm),
+                                    dg.PROBLEMS[pb])
+    if tables is not None:
+        o.set_tables(tables)
+    return o.step(c0, nsteps, 0, lim, cfl)
+
+
+def test_tensor_path_limiter_matches_oracle(dglib, oracle_mod):
+    """Four-quadrant Riemann problem, p = 3, limiter on, transmissive sides."""
+    dg = dglib
+    mesh = dg.Mesh.square(16, 16, jitter=0.1, seed=3, bc=(-4, -4, -4, -4))
+    s = dg.Solver(mesh, dg.EULER, 3, problem="euler_riemann4", limiter=1, cfl=0.2)
+    assert s.tensor_contractions
+    s.init_conditions()
+    c0 = s.get_state()
+    t = s.step(8, dg.SSP_RK3, 0.0)
+    c, to, n = _oracle_run(dg, oracle_mod, mesh, 3, (), "euler_riemann4", c0, 8, 1, 0.2)
+    assert n == 8 and abs(t - to) <= 1e-12 * to
+    assert relerr(s.get_state(), c, 4) <= 1e-10
+
+
+def test_tensor_path_reflecting_walls_and_reference_tables(dglib, oracle_mod):
+    """Slip walls (reflected ghost states) and the reference's own basis
+    tabulation loaded through dg_solver_set_tables: the tensor tables are
+    rebuilt from it, and the run matches the oracle with the same tables."""
+    dg = dglib
+    mesh = dg.Mesh.square(12, 12, box=(0, 10, 0, 10), jitter=0.15, seed=6, bc=(-1, -1, -1, -1))
+    s = dg.Solver(mesh, dg.EULER, 3, problem="euler_vortex", prm=VTX, cfl=0.2)
+    tab = ref_tables(3)
+    s.set_tables(*split_tables(tab, 3))
+    assert s.tensor_contractions
+    s.init_conditions()
+    c0 = s.get_state()
+    t = s.step(10, dg.SSP_RK3, 0.0)
+    c, to, _ = _oracle_run(dg, oracle_mod, mesh, 3, VTX, "euler_vortex", c0, 10, 0, 0.2, tab)
+    assert abs(t - to) <= 1e-12 * to
+    assert relerr(s.get_state(), c, 4) <= 1e-10
