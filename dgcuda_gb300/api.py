@@ -107,6 +107,7 @@ def _declare(L):
         "dg_eval_vertices_view": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, _dp]),
         "dg_save_checkpoint": (C.c_int, [C.c_void_p, C.c_char_p, C.c_double]),
         "dg_set_tensor_contractions": (C.c_int, [C.c_void_p, C.c_int]),
+        "dg_oz_table_image": (C.c_int, [C.c_int, C.c_void_p, C.c_size_t, _dp]),
         "dg_get_tensor_contractions": (C.c_int, [C.c_void_p, _ip]),
         "dg_load_checkpoint": (C.c_int, [C.c_void_p, C.c_char_p, _dp]),
         "dg_set_bathymetry": (C.c_int, [C.c_void_p, _dp]),
@@ -226,6 +227,19 @@ def probe_reciprocal(x, device=0):
     r, q = np.empty_like(x), np.empty_like(x)
     _check(L.dg_probe_reciprocal(device, x.size, _dptr(x), _dptr(r), _dptr(q)))
     return r, q
+
+
+def oz_table_image(p):
+    """(words uint32[2240, 2], colexp int32[3, 16], dense float64[5, 16, 16])
+    of the tensor-core digit tables of order p: the digit words, the column
+    exponents and the tables they were split from (host-built; no GPU
+    needed)."""
+    L = load_library()
+    buf = np.zeros(18176 // 4, dtype=np.uint32)
+    dense = np.zeros((5, 16, 16))
+    _check(L.dg_oz_table_image(p, buf.ctypes.data_as(C.c_void_p), buf.nbytes, _dptr(dense)))
+    return (buf[:4480].reshape(2240, 2).copy(),
+            buf[4480:4528].view(np.int32).reshape(3, 16).copy(), dense)
 
 
 def measure_fp64_peak(device=0):

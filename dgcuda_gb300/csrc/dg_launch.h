@@ -134,7 +134,7 @@ const Ops &ops_euler();
 // tensor-core element stage (Euler, p = 1..4): table image size, builder
 // from the host Tab<p> image, and the per-device kernel attribute
 size_t oz_tabs_bytes();
-bool oz_build_tabs(int p, const void *tabimg, void *out);
+bool oz_build_tabs(int p, const void *tabimg, void *out, double *dense = nullptr);
 cudaError_t oz_prepare_euler(int p);
 const Ops &ops_shallow_water();
 const Ops &ops_maxwell();

@@ -1,6 +1,10 @@
 // dg_ozaki.cu -- host side of the tensor-core contractions: the f16 digit
 // words and column exponents of the element kernel's four basis tables.
 #include <cstring>
+#include <vector>
+
+#include "dg_internal.h"
+#include "dg_tables_data.h"
 
 #include "dg_ozaki.cuh"
 
@@ -65,48 +69,64 @@ int slot(int item) { return slot_of(item / 4, item % 4); }
 
 }  // namespace
 
+// the three tables as dense [K block][K slot][N slot] matrices of doubles:
+// EVAL (1 block), PROJ (3), TRACE (1), in that order (5 x 16 x 16)
 template <int P>
-void build_tabs(const Tab<P> &tb, Tabs *out) {
+void dense_tables(const Tab<P> &tb, double (*T)[16][16]) {
   constexpr int NP = Tab<P>::NP, NQ = Tab<P>::NQ, N1 = Tab<P>::N1;
-  static double T[3][16][16];
-  std::memset(out, 0, sizeof *out);
-  // EVAL: u(q) = sum_i c_i B[q][i]
-  std::memset(T, 0, sizeof T);
-  for (int q = 0; q < NQ; q++)
-    for (int i = 0; i < NP; i++) T[0][slot(i)][slot(q)] = tb.B[q][i];
-  split_table(T, 1, out->w + word_off(kEval), out->colexp[kEval]);
-  // PROJ: r_i = sum_q GR[q][i] g_q + GS[q][i] h_q + sum_fj E[f][j][i] F_fj
-  std::memset(T, 0, sizeof T);
+  std::memset(T, 0, sizeof(double) * 5 * 16 * 16);
   for (int q = 0; q < NQ; q++)
     for (int i = 0; i < NP; i++) {
-      T[0][slot(q)][slot(i)] = tb.GR[q][i];
-      T[1][slot(q)][slot(i)] = tb.GS[q][i];
+      T[0][slot(i)][slot(q)] = tb.B[q][i];    // EVAL: u(q) = sum_i c_i B[q][i]
+      T[1][slot(q)][slot(i)] = tb.GR[q][i];   // PROJ: sum_q GR g_q + GS h_q
+      T[2][slot(q)][slot(i)] = tb.GS[q][i];
     }
   for (int f = 0; f < 3; f++)
     for (int j = 0; j < N1; j++)
-      for (int i = 0; i < NP; i++) T[2][slot(f * N1 + j)][slot(i)] = tb.E[f][j][i];
-  split_table(T, 3, out->w + word_off(kProj), out->colexp[kProj]);
-  // TRACE: u_fj = sum_i E[f][j][i] c_i
-  std::memset(T, 0, sizeof T);
-  for (int f = 0; f < 3; f++)
-    for (int j = 0; j < N1; j++)
-      for (int i = 0; i < NP; i++) T[0][slot(i)][slot(f * N1 + j)] = tb.E[f][j][i];
-  split_table(T, 1, out->w + word_off(kTrace), out->colexp[kTrace]);
+      for (int i = 0; i < NP; i++) {
+        T[3][slot(f * N1 + j)][slot(i)] = tb.E[f][j][i];  // PROJ: + sum_fj E F_fj
+        T[4][slot(i)][slot(f * N1 + j)] = tb.E[f][j][i];  // TRACE: u_fj = sum_i E c_i
+      }
+}
+
+template <int P>
+void build_tabs(const Tab<P> &tb, Tabs *out, double *dense) {
+  static double T[5][16][16];
+  dense_tables<P>(tb, T);
+  if (dense) std::memcpy(dense, T, sizeof T);
+  std::memset(out, 0, sizeof *out);
+  split_table(T, 1, out->w + word_off(kEval), out->colexp[kEval]);
+  split_table(T + 1, 3, out->w + word_off(kProj), out->colexp[kProj]);
+  split_table(T + 4, 1, out->w + word_off(kTrace), out->colexp[kTrace]);
 }
 
 }  // namespace oz
 
 size_t oz_tabs_bytes() { return sizeof(oz::Tabs); }
 
-bool oz_build_tabs(int p, const void *tabimg, void *out) {
+bool oz_build_tabs(int p, const void *tabimg, void *out, double *dense) {
   oz::Tabs *o = static_cast<oz::Tabs *>(out);
   switch (p) {
-    case 1: oz::build_tabs<1>(*static_cast<const Tab<1> *>(tabimg), o); return true;
-    case 2: oz::build_tabs<2>(*static_cast<const Tab<2> *>(tabimg), o); return true;
-    case 3: oz::build_tabs<3>(*static_cast<const Tab<3> *>(tabimg), o); return true;
-    case 4: oz::build_tabs<4>(*static_cast<const Tab<4> *>(tabimg), o); return true;
+    case 1: oz::build_tabs<1>(*static_cast<const Tab<1> *>(tabimg), o, dense); return true;
+    case 2: oz::build_tabs<2>(*static_cast<const Tab<2> *>(tabimg), o, dense); return true;
+    case 3: oz::build_tabs<3>(*static_cast<const Tab<3> *>(tabimg), o, dense); return true;
+    case 4: oz::build_tabs<4>(*static_cast<const Tab<4> *>(tabimg), o, dense); return true;
     default: return false;
   }
 }
 
 }  // namespace dg
+
+// the tensor-core table image of order p (1..4) built from the library's
+// exact basis tables: 2240 uint2 digit words, then 3 x 16 int column
+// exponents (and 16 ints of padding); bytes must be at least that size.
+// dense (optional, 1280 doubles): the tables that were split, as dense
+// [K block][K slot][N slot] matrices (EVAL, PROJ x 3, TRACE)
+extern "C" dg_status dg_oz_table_image(int p, void *out, size_t bytes, double *dense) {
+  if (p < 1 || p > 4 || !out) return dg::fail(DG_BAD_ARG, "order must be 1..4");
+  if (bytes < sizeof(dg::oz::Tabs)) return dg::fail(DG_BAD_ARG, "buffer too small");
+  std::vector<char> tab(dg::tab_bytes(p));
+  dg::build_tab(p, DG_TABLES[p], tab.data());
+  dg::oz_build_tabs(p, tab.data(), out, dense);
+  return DG_OK;
+}

@@ -651,7 +651,7 @@ __global__ void __launch_bounds__(kOzThreads) k_trace_oz(const __grid_constant__
 
 // host: the f16 digit words and column exponents of the four tables
 template <int P>
-void build_tabs(const Tab<P> &tb, Tabs *out);
+void build_tabs(const Tab<P> &tb, Tabs *out, double *dense);
 
 }  // namespace oz
 }  // namespace dg

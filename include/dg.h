@@ -188,6 +188,13 @@ dg_status dg_eval_vertices_view(dg_solver *s, int var, int view, double t, doubl
  * default at p = 2..4 (at p = 1 the FP64 kernel is faster); DG_UNSUPPORTED
  * elsewhere.  No reference counterpart. */
 dg_status dg_set_tensor_contractions(dg_solver *s, int on);
+/* the digit tables of that path for order p = 1..4, built on the host from
+ * the library's basis tables (for checks; no GPU needed): 2240 pairs of
+ * 32-bit words, each two f16 digits, then 3 x 16 int column exponents and 16
+ * ints of padding -- bytes >= 18176.  dense (optional, 1280 doubles): the
+ * tables that were split, as [K block][K slot][N slot] matrices (EVAL,
+ * PROJ x 3, TRACE) */
+dg_status dg_oz_table_image(int p, void *out, size_t bytes, double *dense);
 dg_status dg_get_tensor_contractions(dg_solver *s, int *on);
 
 /* binary checkpoint / restart (no reference counterpart: the reference's
