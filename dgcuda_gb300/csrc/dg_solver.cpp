@@ -1333,16 +1333,20 @@ dg_status amalloc(dg_adjoint *a, T **p, size_t n) {
   return DG_OK;
 }
 
-// one SSP-RK3 step of fixed dt through the unfused stages; keeps the stage
-// inputs u1, u2 when given (bit-identical to dg_step's fused stages)
-void plain_step(dg_solver *s, double *u1keep, double *u2keep) {
+// one SSP-RK3 step of fixed dt through the fused stages (the adjoint
+// excludes the limiter, and without it a fused stage gives the bits of the
+// unfused one: its element epilogue writes the traces k_trace would compute);
+// keeps the stage inputs u1, u2 when given.  T must hold the traces of U, or
+// need_trace asks for them (the first step of a run or of a segment).
+void plain_step(dg_solver *s, double *u1keep, double *u2keep, bool need_trace) {
   const size_t bytes = s->ndof_p * sizeof(double);
   const double *dt = &s->ds->dt;
-  stage(s, s->U, nullptr, s->W, 0.0, 1.0, 1.0, 0.0, dt);
+  if (need_trace) run(s, K_TRACE, [&] { s->ops->trace(s->ctx, s->U); });
+  fused_stage(s, s->U, nullptr, s->W, 0.0, 1.0, 1.0, 0.0, dt);
   if (u1keep) cudaMemcpyAsync(u1keep, s->W, bytes, cudaMemcpyDeviceToDevice, s->st);
-  stage(s, s->W, s->U, s->W, 0.75, 0.25, 0.25, 1.0, dt);
+  fused_stage(s, s->W, s->U, s->W, 0.75, 0.25, 0.25, 1.0, dt);
   if (u2keep) cudaMemcpyAsync(u2keep, s->W, bytes, cudaMemcpyDeviceToDevice, s->st);
-  stage(s, s->W, s->U, s->U, 1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0, 0.5, dt);
+  fused_stage(s, s->W, s->U, s->U, 1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0, 0.5, dt);
   run(s, K_CFL, [&] { dg::launch_advance_t(s->st, s->ds); });
 }
 
@@ -1475,7 +1479,7 @@ extern "C" dg_status dg_adjoint_forward(dg_adjoint *a, int nsteps, double dt, in
   for (int n = 0; n < nsteps; n++) {
     if (n % ckpt == 0)
       CK(cudaMemcpyAsync(a->cks[n / ckpt], s->U, bytes, cudaMemcpyDeviceToDevice, s->st));
-    plain_step(s, nullptr, nullptr);
+    plain_step(s, nullptr, nullptr, n == 0);
     if ((n + 1) % every == 0)
       dg::launch_sample(s->st, s->U, a->rec_el, a->rec_phi, a->nrec, s->np, s->m.Kp,
                         a->samples + (size_t)((n + 1) / every - 1) * a->nrec);
@@ -1524,7 +1528,7 @@ extern "C" dg_status dg_adjoint_backward(dg_adjoint *a, const double *sbar, doub
     for (int m = n0; m < n1; m++) {
       const int j = m - n0;
       CK(cudaMemcpyAsync(a->seg[3 * j], s->U, bytes, cudaMemcpyDeviceToDevice, s->st));
-      plain_step(s, a->seg[3 * j + 1], a->seg[3 * j + 2]);
+      plain_step(s, a->seg[3 * j + 1], a->seg[3 * j + 2], m == n0);
     }
     for (int m = n1 - 1; m >= n0; m--) {
       const int j = m - n0;
@@ -1558,7 +1562,8 @@ extern "C" dg_status dg_adjoint_backward(dg_adjoint *a, const double *sbar, doub
   // leave the solver at the final state of the forward run
   CK(cudaMemcpyAsync(s->U, a->cks[nck - 1], bytes, cudaMemcpyDeviceToDevice, s->st));
   if ((st = set_fixed_dt(s, a->t0 + (nck - 1) * a->ckpt * dt, dt)) != DG_OK) return st;
-  for (int m = (nck - 1) * a->ckpt; m < a->nsteps; m++) plain_step(s, nullptr, nullptr);
+  for (int m = (nck - 1) * a->ckpt; m < a->nsteps; m++)
+    plain_step(s, nullptr, nullptr, m == (nck - 1) * a->ckpt);
   collect_profile(s);
   return sync_check(s);
 }

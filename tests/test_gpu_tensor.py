@@ -150,3 +150,29 @@ def test_tensor_path_reflecting_walls_and_reference_tables(dglib, oracle_mod):
     c, to, _ = _oracle_run(dg, oracle_mod, mesh, 3, VTX, "euler_vortex", c0, 10, 0, 0.2, tab)
     assert abs(t - to) <= 1e-12 * to
     assert relerr(s.get_state(), c, 4) <= 1e-10
+
+
+def test_full_size_conservation_determinism_and_fp64_agreement(dglib):
+    """The bench problem at its full size (1024 x 1024 squares, 2,097,152
+    triangles, p = 3, limiter on) with periodic sides, so that the element
+    means' total is conserved: 3 steps on the tensor path conserve every
+    variable to rounding, repeat bit for bit, and agree with the FP64
+    kernel to rounding."""
+    dg = dglib
+    mesh = dg.Mesh.square(1024, 1024, jitter=0.1, seed=3)
+    V = mesh.arrays()[0]
+    J = (V[2] - V[0]) * (V[5] - V[1]) - (V[4] - V[0]) * (V[3] - V[1])
+    outs = []
+    for tensor in (True, True, False):
+        s = dg.Solver(mesh, dg.EULER, 3, problem="euler_riemann4", limiter=1, cfl=0.2)
+        s.tensor_contractions = tensor
+        s.init_conditions()
+        m0 = (s.get_state()[:, 0, :] * J).sum(axis=1)
+        s.step(3, dg.SSP_RK3, 0.0)
+        c = s.get_state()
+        m1 = (c[:, 0, :] * J).sum(axis=1)
+        assert np.all(np.abs(m1 - m0) <= 1e-12 * np.abs(m0).max())
+        outs.append(c)
+        s.close()
+    assert np.array_equal(outs[0], outs[1])
+    assert relerr(outs[0], outs[2], 4) <= 1e-12
