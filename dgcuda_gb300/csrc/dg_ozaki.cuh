@@ -231,6 +231,11 @@ __device__ __forceinline__ double recombine(const Acc &acc, int cg, int r, int m
   return ldexp(neg ? -v : v, k);
 }
 
+// a hint that the line holding p will be read soon (no register is held)
+__device__ __forceinline__ void prefetch_l1(const void *p) {
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
 // largest biased exponent over a quad's row (all 4 lanes hold the result)
 __device__ __forceinline__ int quad_max(int m) {
   m = max(m, __shfl_xor_sync(0xffffffffu, m, 1));
@@ -303,6 +308,13 @@ __global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_const
   // ---- area-point values of every variable -> ub ----
 #pragma unroll 1
   for (int n = 0; n < N; n++) {
+    if (n + 1 < N) {  // the next variable's coefficients
+#pragma unroll
+      for (int e = 0; e < 2; e++)
+#pragma unroll
+        for (int p = 0; p < PM; p++)
+          if (p * 4 + t < NP) prefetch_l1(us + (size_t)((n + 1) * NP + p * 4 + t) * Kp + ec[e]);
+    }
     double x[2][4];
 #pragma unroll
     for (int e = 0; e < 2; e++)
@@ -355,6 +367,31 @@ __global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_const
     }
   }
 
+  // ---- side-flux offsets and signs of the element's edge points ----
+  int foff[PF][2];
+  double fsg[PF][2];
+#pragma unroll
+  for (int p = 0; p < PF; p++)
+#pragma unroll
+    for (int e = 0; e < 2; e++) {
+      const int idx = p * 4 + t;
+      if (idx < NF) {
+        const int f = idx / N1, j = idx % N1;
+        const int sd = a.esd[(size_t)f * Kp + ec[e]];
+        const bool right = sd & 1;
+        foff[p][e] = (sd >> 1) * (N1 * N) + (right ? (N1 - 1 - j) : j) * N;
+        fsg[p][e] = right ? 1.0 : -1.0;
+      } else {
+        foff[p][e] = 0;
+        fsg[p][e] = 0.0;
+      }
+    }
+#pragma unroll
+  for (int p = 0; p < PF; p++)
+#pragma unroll
+    for (int e = 0; e < 2; e++)
+      if (p * 4 + t < NF) prefetch_l1(a.Fh + foff[p][e]);  // read in the projection
+
   // ---- fluxes folded with the metric -> gh ----
   const double *geo = a.geo;
   double sc[2];
@@ -384,29 +421,19 @@ __global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_const
     }
   }
 
-  // ---- side-flux offsets and signs of the element's edge points ----
-  int foff[PF][2];
-  double fsg[PF][2];
-#pragma unroll
-  for (int p = 0; p < PF; p++)
-#pragma unroll
-    for (int e = 0; e < 2; e++) {
-      const int idx = p * 4 + t;
-      if (idx < NF) {
-        const int f = idx / N1, j = idx % N1;
-        const int sd = a.esd[(size_t)f * Kp + ec[e]];
-        const bool right = sd & 1;
-        foff[p][e] = (sd >> 1) * (N1 * N) + (right ? (N1 - 1 - j) : j) * N;
-        fsg[p][e] = right ? 1.0 : -1.0;
-      } else {
-        foff[p][e] = 0;
-        fsg[p][e] = 0.0;
-      }
-    }
-
   // ---- per variable: projection, surface, RK combination, traces -> ub ----
 #pragma unroll 1
   for (int n = 0; n < N; n++) {
+    // this variable's stage input and u^n for the RK combination
+#pragma unroll
+    for (int e = 0; e < 2; e++)
+#pragma unroll
+      for (int p = 0; p < PM; p++)
+        if (p * 4 + t < NP) {
+          const size_t o = (size_t)(n * NP + p * 4 + t) * Kp + ec[e];
+          prefetch_l1(us + o);
+          if (a.ca != 0.0) prefetch_l1(a.un + o);
+        }
     double R[PM][2];
     {  // volume (K blocks GR, GS over the area points) and surface (K block E
        // over the edge points) into one accumulator when the exactness
