@@ -305,6 +305,14 @@ __global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_const
   const uint2 *W = ozt->w;
   Acc acc;
 
+  // geometry and side indices, read after the first contractions
+#pragma unroll
+  for (int e = 0; e < 2; e++) {
+#pragma unroll
+    for (int r = 0; r < 5; r++) prefetch_l1(a.geo + (size_t)r * Kp + ec[e]);
+#pragma unroll
+    for (int f = 0; f < 3; f++) prefetch_l1(a.esd + (size_t)f * Kp + ec[e]);
+  }
   // ---- area-point values of every variable -> ub ----
 #pragma unroll 1
   for (int n = 0; n < N; n++) {
