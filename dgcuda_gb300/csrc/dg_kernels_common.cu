@@ -79,6 +79,25 @@ void launch_permute_in(cudaStream_t st, const double *user, double *internal, co
   if (n) k_permute_in<<<grid_for(n), kB, 0, st>>>(user, internal, perm, rows, K, Kp);
 }
 
+// permute_in that also sets *changed when any value differs (bitwise) from
+// the one it overwrites
+__global__ void k_permute_in_cmp(const double *__restrict__ user, double *__restrict__ in,
+                                 const int *__restrict__ perm, int rows, int K, int Kp,
+                                 int *changed) {
+  size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (size_t)rows * Kp) return;
+  int r = (int)(idx / Kp), e = (int)(idx % Kp);
+  const double v = e < K ? user[(size_t)r * K + perm[e]] : 0.0;
+  if (__double_as_longlong(in[idx]) != __double_as_longlong(v)) *changed = 1;
+  in[idx] = v;
+}
+
+void launch_permute_in_cmp(cudaStream_t st, const double *user, double *internal,
+                           const int *perm, int rows, int K, int Kp, int *changed) {
+  size_t n = (size_t)rows * Kp;
+  if (n) k_permute_in_cmp<<<grid_for(n), kB, 0, st>>>(user, internal, perm, rows, K, Kp, changed);
+}
+
 void launch_permute_out(cudaStream_t st, const double *internal, double *user, const int *perm,
                         int rows, int K, int Kp) {
   size_t n = (size_t)rows * K;

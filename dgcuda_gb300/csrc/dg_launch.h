@@ -146,6 +146,8 @@ void build_tab(int p, const dg_order_tables &src, void *dst);
 // helpers (dg_kernels_common.cu)
 void launch_permute_in(cudaStream_t st, const double *user, double *internal, const int *perm,
                        int rows, int K, int Kp);
+void launch_permute_in_cmp(cudaStream_t st, const double *user, double *internal,
+                           const int *perm, int rows, int K, int Kp, int *changed);
 void launch_permute_out(cudaStream_t st, const double *internal, double *user, const int *perm,
                         int rows, int K, int Kp);
 // y = a * x + b * y over n entries (RK4 / RK2 combinations), dt-scaled when dts != 0

@@ -50,6 +50,7 @@ struct dg_solver {
   double *lin_tv = nullptr, *lin_f0 = nullptr, *lin_f1 = nullptr;  // adjoint work
   bool has_inout_bc = false;      // a side with an inflow or outflow code
   void *oz = nullptr;             // tensor-core tables (Euler, p = 1..4)
+  int *flag = nullptr;            // device flag of put_state
   bool tensor = true;             // use them in the fused element stage
   // T holds the traces of U as the last fused SSP-RK3 stage left them (and U
   // is already limited): the next dg_step continues without recomputing
@@ -675,14 +676,36 @@ extern "C" dg_status dg_init(dg_solver *s) {
   return sync_check(s);
 }
 
+// writes the state; when the stored traces were current and the new state
+// is bitwise the old one (a state read out and handed back unchanged), they
+// stay current, so the next dg_step continues exactly as if the state had
+// never left the device
+static dg_status put_state(dg_solver *s, const double *user) {
+  const bool keep = s->tr_valid;
+  s->tr_valid = false;
+  if (!keep) {
+    dg::launch_permute_in(s->st, user, s->U, s->m.perm, s->N * s->np, s->K, s->m.Kp);
+    return sync_check(s);
+  }
+  if (!s->flag) {
+    dg_status st = dalloc(s, &s->flag, 1);
+    if (st != DG_OK) return st;
+  }
+  CK(cudaMemsetAsync(s->flag, 0, sizeof(int), s->st));
+  dg::launch_permute_in_cmp(s->st, user, s->U, s->m.perm, s->N * s->np, s->K, s->m.Kp, s->flag);
+  int changed = 1;
+  CK(cudaMemcpyAsync(&changed, s->flag, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+  dg_status st = sync_check(s);
+  if (st == DG_OK) s->tr_valid = changed == 0;
+  return st;
+}
+
 extern "C" dg_status dg_set_state(dg_solver *s, const double *C) {
   if (!s || !C) return fail(DG_BAD_ARG, "null argument");
-  s->tr_valid = false;
   CK(cudaSetDevice(s->device));
   size_t n = (size_t)s->N * s->np * s->K;
   CK(cudaMemcpyAsync(s->ubuf, C, n * sizeof(double), cudaMemcpyHostToDevice, s->st));
-  dg::launch_permute_in(s->st, s->ubuf, s->U, s->m.perm, s->N * s->np, s->K, s->m.Kp);
-  return sync_check(s);
+  return put_state(s, s->ubuf);
 }
 
 extern "C" dg_status dg_get_state(dg_solver *s, double *C) {
@@ -696,10 +719,8 @@ extern "C" dg_status dg_get_state(dg_solver *s, double *C) {
 
 extern "C" dg_status dg_set_state_device(dg_solver *s, const double *C) {
   if (!s || !C) return fail(DG_BAD_ARG, "null argument");
-  s->tr_valid = false;
   CK(cudaSetDevice(s->device));
-  dg::launch_permute_in(s->st, C, s->U, s->m.perm, s->N * s->np, s->K, s->m.Kp);
-  return sync_check(s);
+  return put_state(s, C);
 }
 
 extern "C" dg_status dg_get_state_device(dg_solver *s, double *C) {
