@@ -305,9 +305,11 @@ __global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_const
   const uint2 *W = ozt->w;
   Acc acc;
 
-  // geometry and side indices, read after the first contractions
+  // geometry and side indices, read after the first contractions (the
+  // prefetches pay from p = 3 on; at p <= 2 they cost more than they save)
+  constexpr bool kPrefetch = P >= 3;
 #pragma unroll
-  for (int e = 0; e < 2; e++) {
+  for (int e = 0; e < 2 && kPrefetch; e++) {
 #pragma unroll
     for (int r = 0; r < 5; r++) prefetch_l1(a.geo + (size_t)r * Kp + ec[e]);
 #pragma unroll
@@ -316,7 +318,7 @@ __global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_const
   // ---- area-point values of every variable -> ub ----
 #pragma unroll 1
   for (int n = 0; n < N; n++) {
-    if (n + 1 < N) {  // the next variable's coefficients
+    if (kPrefetch && n + 1 < N) {  // the next variable's coefficients
 #pragma unroll
       for (int e = 0; e < 2; e++)
 #pragma unroll
@@ -398,7 +400,7 @@ __global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_const
   for (int p = 0; p < PF; p++)
 #pragma unroll
     for (int e = 0; e < 2; e++)
-      if (p * 4 + t < NF) prefetch_l1(a.Fh + foff[p][e]);  // read in the projection
+      if (kPrefetch && p * 4 + t < NF) prefetch_l1(a.Fh + foff[p][e]);  // read in the projection
 
   // ---- fluxes folded with the metric -> gh ----
   const double *geo = a.geo;
@@ -437,7 +439,7 @@ __global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_const
     for (int e = 0; e < 2; e++)
 #pragma unroll
       for (int p = 0; p < PM; p++)
-        if (p * 4 + t < NP) {
+        if (kPrefetch && p * 4 + t < NP) {
           const size_t o = (size_t)(n * NP + p * 4 + t) * Kp + ec[e];
           prefetch_l1(us + o);
           if (a.ca != 0.0) prefetch_l1(a.un + o);
