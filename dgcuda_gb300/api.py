@@ -12,6 +12,7 @@ BC_REFLECT, BC_OUTFLOW, BC_INFLOW, BC_TRANSMISSIVE, PERIODIC = -1, -2, -3, -4, 0
 PROBLEMS = {
     "none": 0, "adv_sine": 1, "adv_linear": 2, "euler_vortex": 3, "euler_riemann4": 4,
     "euler_supersonic": 5, "sw_hump": 6, "sw_test": 7, "maxwell_plane": 8,
+    "euler_cylinder": 9, "euler_lshock": 10, "euler_doublemach": 11,
 }
 _NVARS = {ADVECTION: 1, EULER: 4, SHALLOW_WATER: 3, MAXWELL: 3}
 _STATUS = ["OK", "BAD_ARG", "BAD_MESH", "NONPHYSICAL", "NAN", "CUDA_ERROR", "TIMEOUT",

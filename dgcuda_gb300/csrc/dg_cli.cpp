@@ -14,7 +14,8 @@
 //   options that the reference selects at compile time:
 //     --eq advection|euler|shallowwater|maxwell   (equation module)
 //     --problem NAME   (adv_sine, adv_linear, euler_vortex, euler_riemann4,
-//                       euler_supersonic, sw_hump, sw_test, maxwell_plane)
+//                       euler_supersonic, sw_hump, sw_test, maxwell_plane,
+//                       euler_cylinder, euler_lshock, euler_doublemach)
 //     --scheme rk4|rk2|ssprk3   (time_integrator; default rk4)
 //     --limiter        (limiter = LIMITER)
 //     --cfl x          (default: 0.5 for rk4, 0.7 for rk2, 0.3 for ssprk3)
@@ -174,9 +175,10 @@ int main(int argc, char **argv) {
   else if (eq_name == "maxwell") eq = DG_MAXWELL;
   else { usage(); return 1; }
   const char *pbs[] = {"none", "adv_sine", "adv_linear", "euler_vortex", "euler_riemann4",
-                       "euler_supersonic", "sw_hump", "sw_test", "maxwell_plane"};
+                       "euler_supersonic", "sw_hump", "sw_test", "maxwell_plane",
+                       "euler_cylinder", "euler_lshock", "euler_doublemach"};
   prm.problem = -1;
-  for (int k = 0; k < 9; k++)
+  for (int k = 0; k < 12; k++)
     if (problem == pbs[k]) prm.problem = k;
   if (prm.problem < 0) { usage(); return 1; }
   dg_scheme scheme;

@@ -37,8 +37,34 @@ struct Tab {
 
 enum Problem {
   PB_NONE = 0, PB_ADV_SINE = 1, PB_ADV_LINEAR = 2, PB_EULER_VORTEX = 3, PB_EULER_RIEMANN4 = 4,
-  PB_EULER_SUPERSONIC = 5, PB_SW_HUMP = 6, PB_SW_TEST = 7, PB_MAXWELL_PLANE = 8
+  PB_EULER_SUPERSONIC = 5, PB_SW_HUMP = 6, PB_SW_TEST = 7, PB_MAXWELL_PLANE = 8,
+  PB_EULER_CYLINDER = 9, PB_EULER_LSHOCK = 10, PB_EULER_DOUBLEMACH = 11
 };
+
+// double Mach reflection (euler/doublemach/doublemach.cu): the wall starts at
+// x = 1/6; the post-shock state (rho 8, speed 8.25 at -30 degrees, p 116.5)
+// and the quiescent gas (rho = gamma, p = 1)
+constexpr double kDmX0 = 0.16666666666666666;
+DG_HD void dm_shock(const EqP &q, double *U) {
+  const double c = 0.86602540378443864676, s = 0.5;  // cos, sin of 30 degrees
+  U[0] = 8.;
+  U[1] = 8.25 * c * U[0];
+  U[2] = -8.25 * s * U[0];
+  U[3] = fma(0.5 * U[0], 8.25 * 8.25, 116.5 / (q.gamma - 1.0));
+}
+DG_HD void dm_rest(const EqP &q, double *U) {
+  U[0] = q.gamma;
+  U[1] = 0.;
+  U[2] = 0.;
+  U[3] = 1. / (q.gamma - 1.0);
+}
+// uniform flow along x at Mach M (cylinder.cu, lshock.cu: rho = gamma, p = 1)
+DG_HD void uniform_mach(const EqP &q, double M, double *U) {
+  U[0] = q.gamma;
+  U[1] = U[0] * M;
+  U[2] = 0.;
+  U[3] = fma(0.5 * U[0], M * M, 1. / (q.gamma - 1.0));
+}
 
 constexpr double kPi = 3.141592653589793238462643383279502884;
 
@@ -139,6 +165,16 @@ DG_HD void exact_state(const EqP &q, double *U, double x, double y, double t) {
       U[1] = 0;
       U[2] = 0;
       break;
+    case PB_EULER_CYLINDER:  // cylinder.cu:23-45: U0 = U_inflow = U_outflow, Mach 0.38
+      uniform_mach(q, P[0] != 0 ? P[0] : 0.38, U);
+      break;
+    case PB_EULER_LSHOCK:  // lshock.cu:23-45, Mach 2
+      uniform_mach(q, P[0] != 0 ? P[0] : 2.0, U);
+      break;
+    case PB_EULER_DOUBLEMACH:  // doublemach.cu:55-70: U_inflow = U_outflow
+      if (x < kDmX0 + (1. + 20. * t) / sqrt(3.)) dm_shock(q, U);
+      else dm_rest(q, U);
+      break;
     case PB_MAXWELL_PLANE: {  // plane TM wave along x
       double c = 1 / sqrt(q.mu * q.eps);
       double ez = sin(2 * kPi * (x - c * t));
@@ -150,6 +186,18 @@ DG_HD void exact_state(const EqP &q, double *U, double x, double y, double t) {
     default:
       U[0] = U[1] = U[2] = U[3] = 0;
   }
+}
+
+// the initial state (U0): the exact state at t = 0, except where a problem's
+// initial data differ from its boundary data
+DG_HD void init_state(const EqP &q, double *U, double x, double y) {
+  if (q.problem == PB_EULER_DOUBLEMACH) {  // doublemach.cu:41-52: shock at 60 degrees
+    const double angle = atan(y / (x - kDmX0));
+    if (angle > 60. * kPi / 180 || x < kDmX0) dm_shock(q, U);
+    else dm_rest(q, U);
+    return;
+  }
+  exact_state(q, U, x, y, 0.0);
 }
 
 // --------------------------------------------------------------------------
@@ -233,7 +281,10 @@ struct Euler {  // euler/euler.cu
   }
   DG_HD static void reflect(const EqP &q, const double *UL, double *UR, double x, double y,
                             double nx, double ny) {
-    if (q.problem == PB_EULER_SUPERSONIC) {  // supersonic.cu:65-87, curved wall
+    if (q.problem == PB_EULER_DOUBLEMACH && x < kDmX0) {  // doublemach.cu:75-93
+      dm_shock(q, UR);
+    } else if (q.problem == PB_EULER_SUPERSONIC || q.problem == PB_EULER_CYLINDER) {
+      // curved wall around the origin (supersonic.cu:65-87, cylinder.cu:55-80)
       double d = sqrt(fma(x, x, y * y)), Nx = x / d, Ny = y / d;
       if (Nx * nx + Ny * ny < 0) {
         Nx = -Nx;

@@ -575,7 +575,7 @@ __global__ void __launch_bounds__(kBlock) k_init(const __grid_constant__ Tab<P> 
     const double x = V[2] * r + V[4] * s + V[0] * (1 - r - s);
     const double y = V[3] * r + V[5] * s + V[1] * (1 - r - s);
     double U0[4];
-    exact_state(q, U0, x, y, 0.0);
+    init_state(q, U0, x, y);
 #pragma unroll
     for (int i = 0; i < NP; i++)
 #pragma unroll

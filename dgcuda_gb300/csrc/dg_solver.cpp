@@ -402,7 +402,7 @@ extern "C" dg_status dg_solver_create(const dg_mesh *mesh, dg_equation eq, int p
   dg_params P;
   if (prm) P = *prm;
   else dg_params_default(&P);
-  if (P.problem < 0 || P.problem > DG_PB_MAXWELL_PLANE) return fail(DG_BAD_ARG, "unknown problem");
+  if (P.problem < 0 || P.problem > DG_PB_EULER_DOUBLEMACH) return fail(DG_BAD_ARG, "unknown problem");
   if (!(P.cfl > 0)) return fail(DG_BAD_ARG, "cfl must be positive");
   if (eq == DG_EULER && !(P.gamma > 1)) return fail(DG_BAD_ARG, "gamma must be > 1");
   if (eq == DG_SHALLOW_WATER && !(P.gravity > 0)) return fail(DG_BAD_ARG, "gravity must be > 0");

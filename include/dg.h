@@ -54,7 +54,12 @@ typedef enum {
   DG_PB_EULER_SUPERSONIC = 5, /* supersonic vortex (euler/supersonic/supersonic.cu) */
   DG_PB_SW_HUMP = 6,        /* still water hump: prm h0, A, sigma, x0, y0 */
   DG_PB_SW_TEST = 7,        /* shallowwater/test/test.cu hump */
-  DG_PB_MAXWELL_PLANE = 8   /* plane TM wave along x */
+  DG_PB_MAXWELL_PLANE = 8,  /* plane TM wave along x */
+  DG_PB_EULER_CYLINDER = 9, /* uniform flow past a cylinder at the origin (euler/cylinder):
+                               prm[0] Mach (0: 0.38); walls are the circle through the point */
+  DG_PB_EULER_LSHOCK = 10,  /* uniform flow with slip walls (euler/lshock): prm[0] Mach (0: 2) */
+  DG_PB_EULER_DOUBLEMACH = 11 /* double Mach reflection (euler/doublemach): a Mach 10 shock
+                               at 60 degrees; the wall reflects from x = 1/6 on */
 } dg_problem;
 
 /* boundary codes in the .pmsh right-element column (genmesh.py:166-174) */

@@ -55,7 +55,8 @@
 enum { EQ_ADV = 0, EQ_EULER = 1, EQ_SW = 2, EQ_MAXWELL = 3 };
 enum {
   PB_NONE = 0, PB_ADV_SINE = 1, PB_ADV_LINEAR = 2, PB_EULER_VORTEX = 3, PB_EULER_RIEMANN4 = 4,
-  PB_EULER_SUPERSONIC = 5, PB_SW_HUMP = 6, PB_SW_TEST = 7, PB_MAXWELL_PLANE = 8
+  PB_EULER_SUPERSONIC = 5, PB_SW_HUMP = 6, PB_SW_TEST = 7, PB_MAXWELL_PLANE = 8,
+  PB_EULER_CYLINDER = 9, PB_EULER_LSHOCK = 10, PB_EULER_DOUBLEMACH = 11
 };
 
 typedef struct or_solver {
@@ -185,6 +186,28 @@ int or_get_tables(const or_solver *o, double *out) {
 }
 
 /* ---------------- problems (initial / boundary / exact states) ---------------- */
+/* double Mach reflection (euler/doublemach/doublemach.cu:20-93) */
+#define DM_X0 0.16666666666666666
+static void dm_shock(const or_solver *o, double *U) {
+  U[0] = 8.;
+  U[1] = 8.25 * 0.86602540378443864676 * U[0];
+  U[2] = -8.25 * 0.5 * U[0];
+  U[3] = 0.5 * U[0] * 8.25 * 8.25 + 116.5 / (o->gamma - 1.0);
+}
+static void dm_rest(const or_solver *o, double *U) {
+  U[0] = o->gamma;
+  U[1] = 0.;
+  U[2] = 0.;
+  U[3] = 1. / (o->gamma - 1.0);
+}
+/* uniform flow along x at Mach M (cylinder.cu:23-45, lshock.cu:23-45) */
+static void uniform_mach(const or_solver *o, double M, double *U) {
+  U[0] = o->gamma;
+  U[1] = U[0] * M;
+  U[2] = 0.;
+  U[3] = 0.5 * U[0] * M * M + 1. / (o->gamma - 1.0);
+}
+
 static void exact_state(const or_solver *o, double *U, double x, double y, double t) {
   const double *P = o->prm;
   switch (o->problem) {
@@ -251,6 +274,16 @@ static void exact_state(const or_solver *o, double *U, double x, double y, doubl
       U[1] = 0;
       U[2] = 0;
       break;
+    case PB_EULER_CYLINDER:
+      uniform_mach(o, P[0] != 0 ? P[0] : 0.38, U);
+      break;
+    case PB_EULER_LSHOCK:
+      uniform_mach(o, P[0] != 0 ? P[0] : 2.0, U);
+      break;
+    case PB_EULER_DOUBLEMACH: /* U_inflow = U_outflow (doublemach.cu:55-70) */
+      if (x < DM_X0 + (1. + 20. * t) / sqrt(3.)) dm_shock(o, U);
+      else dm_rest(o, U);
+      break;
     case PB_MAXWELL_PLANE: {
       double c = 1 / sqrt(o->mu * o->eps);
       double ez = sin(2 * M_PI * (x - c * t));
@@ -262,6 +295,18 @@ static void exact_state(const or_solver *o, double *U, double x, double y, doubl
     default:
       for (int n = 0; n < NMAX; n++) U[n] = 0;
   }
+}
+
+/* the initial state U0: the exact state at t = 0 except where a problem's
+ * initial data differ from its boundary data */
+static void init_state(const or_solver *o, double *U, double x, double y) {
+  if (o->problem == PB_EULER_DOUBLEMACH) { /* doublemach.cu:41-52 */
+    double angle = atan(y / (x - DM_X0));
+    if (angle > 60. * M_PI / 180 || x < DM_X0) dm_shock(o, U);
+    else dm_rest(o, U);
+    return;
+  }
+  exact_state(o, U, x, y, 0.0);
 }
 
 /* ghost state of a boundary side (eval_boundary, conserv_kernels.cu:820-843) */
@@ -282,7 +327,10 @@ static void ghost(const or_solver *o, int code, const double *UL, double *UR, do
   }
   /* reflect */
   if (o->eq == EQ_EULER) {
-    if (o->problem == PB_EULER_SUPERSONIC) { /* supersonic.cu:65-87 */
+    if (o->problem == PB_EULER_DOUBLEMACH && x < DM_X0) { /* doublemach.cu:75-93 */
+      dm_shock(o, UR);
+    } else if (o->problem == PB_EULER_SUPERSONIC || o->problem == PB_EULER_CYLINDER) {
+      /* curved wall around the origin (supersonic.cu:65-87, cylinder.cu:55-80) */
       double d = sqrt(x * x + y * y), Nx = x / d, Ny = y / d;
       if (Nx * nx + Ny * ny < 0) {
         Nx = -Nx;
@@ -810,16 +858,22 @@ int or_step(or_solver *o, double *C, int nsteps, int scheme, int limiter, double
     step++;
     if (scheme == 0) {
       /* u1 = u + dt L(u); u2 = 3/4 u + 1/4 (u1 + dt L(u1));
-       * u = 1/3 u + 2/3 (u2 + dt L(u2)); stage times t, t + dt, t + dt/2 */
+       * u = 1/3 u + 2/3 (u2 + dt L(u2)); stage times t, t + dt, t + dt/2.
+       * Each stage output is limited, then flattened where its traces are
+       * non-physical (the GPU's fused stage does both before the next stage
+       * reads the output, so the state after a step is the flattened one) */
       dg_operator(o, C, t, dt, k1);
       for (size_t i = 0; i < nd; i++) k2[i] = C[i] + k1[i];
       if (limiter) or_limit(o, k2);
+      o->flattened += flatten_pass(o, k2);
       dg_operator(o, k2, t + dt, dt, k1);
       for (size_t i = 0; i < nd; i++) k3[i] = 0.75 * C[i] + 0.25 * (k2[i] + k1[i]);
       if (limiter) or_limit(o, k3);
+      o->flattened += flatten_pass(o, k3);
       dg_operator(o, k3, t + 0.5 * dt, dt, k1);
       for (size_t i = 0; i < nd; i++) C[i] = C[i] / 3. + 2. / 3. * (k3[i] + k1[i]);
       if (limiter) or_limit(o, C);
+      o->flattened += flatten_pass(o, C);
       t += dt;
     } else if (scheme == 1) {
       t += dt;
@@ -865,7 +919,7 @@ int or_init(or_solver *o, double *C) {
       for (int q = 0; q < o->nq; q++) {
         double x, y, u0[NMAX];
         vol_xy(o, e, q, &x, &y);
-        exact_state(o, u0, x, y, 0.0);
+        init_state(o, u0, x, y);
         for (int n = 0; n < N; n++) U[n] += o->w[q] * u0[n] * o->B[q][i];
       }
       for (int n = 0; n < N; n++) C[CI(n, i, e)] = U[n];
