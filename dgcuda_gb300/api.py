@@ -12,7 +12,9 @@ BC_REFLECT, BC_OUTFLOW, BC_INFLOW, BC_TRANSMISSIVE, PERIODIC = -1, -2, -3, -4, 0
 PROBLEMS = {
     "none": 0, "adv_sine": 1, "adv_linear": 2, "euler_vortex": 3, "euler_riemann4": 4,
     "euler_supersonic": 5, "sw_hump": 6, "sw_test": 7, "maxwell_plane": 8,
-    "euler_cylinder": 9, "euler_lshock": 10, "euler_doublemach": 11,
+    "euler_cylinder": 9, "euler_lshock": 10, "euler_doublemach": 11, "euler_airfoil": 12,
+    "adv_squarehill": 13, "adv_rotatinghill": 14, "adv_spin": 15, "maxwell_cmirror": 16,
+    "maxwell_wscatter": 17, "euler_pulse": 18,
 }
 _NVARS = {ADVECTION: 1, EULER: 4, SHALLOW_WATER: 3, MAXWELL: 3}
 _STATUS = ["OK", "BAD_ARG", "BAD_MESH", "NONPHYSICAL", "NAN", "CUDA_ERROR", "TIMEOUT",
@@ -70,6 +72,10 @@ def _declare(L):
         "dg_version": (C.c_char_p, []),
         "dg_last_error": (C.c_char_p, []),
         "dg_params_default": (None, [C.POINTER(Params)]),
+        "dg_params_for_problem": (C.c_int, [C.POINTER(Params), C.c_int, _ip]),
+        "dg_set_velocity_field": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _dp]),
+        "dg_get_velocity_field": (C.c_int, [C.c_void_p, _dp]),
+        "dg_set_inflow_series": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, C.c_double]),
         "dg_mesh_read_pmsh": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
         "dg_mesh_write_pmsh": (C.c_int, [C.c_void_p, C.c_char_p]),
         "dg_mesh_read_gmsh": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
@@ -218,6 +224,18 @@ class Adjoint:
 
     def __del__(self):
         self.close()
+
+
+def params_for_problem(problem):
+    """(Params, scheme): the defaults with the reference problem's own
+    settings (limiter, Mach, angle, velocity, g) and its time integrator."""
+    L = load_library()
+    if isinstance(problem, str):
+        problem = PROBLEMS[problem]
+    prm = Params()
+    sc = np.zeros(1, dtype=np.int32)
+    _check(L.dg_params_for_problem(C.byref(prm), int(problem), _iptr(sc)))
+    return prm, int(sc[0])
 
 
 def probe_reciprocal(x, device=0):
@@ -443,6 +461,29 @@ class Solver:
     @tensor_contractions.setter
     def tensor_contractions(self, on):
         _check(self._L.dg_set_tensor_contractions(self._h, int(bool(on))))
+
+    def set_velocity_field(self, ax, ay, grad=None):
+        """Advection velocity a(x, y) = (ax, ay) + grad (x, y), grad =
+        (dax/dx, dax/dy, day/dx, day/dy) or None (the problem's get_velocity,
+        advection.cu:12)."""
+        g = None if grad is None else np.ascontiguousarray(grad, dtype=np.float64)
+        _check(self._L.dg_set_velocity_field(self._h, float(ax), float(ay),
+                                             None if g is None else _dptr(g)))
+
+    def velocity_field(self):
+        """(ax, ay, grad[4], CFL wave speed)."""
+        out = np.zeros(7)
+        _check(self._L.dg_get_velocity_field(self._h, _dptr(out)))
+        return out[0], out[1], out[2:6].copy(), out[6]
+
+    def set_inflow_series(self, amp, omega, phase, t0=0.0):
+        """Inflow pressure series of euler_pulse: p(t) = 1 + sum amp_k
+        cos(omega_k (t + t0) + phase_k) (the tube / trumpet inflow)."""
+        a, w, f = (np.ascontiguousarray(v, dtype=np.float64) for v in (amp, omega, phase))
+        if not (len(a) == len(w) == len(f)):
+            raise ValueError("amp, omega and phase differ in length")
+        _check(self._L.dg_set_inflow_series(self._h, len(a), _dptr(a), _dptr(w), _dptr(f),
+                                            float(t0)))
 
     def save_checkpoint(self, path, t):
         """Binary state (+ bed) with the time t and a checksum."""

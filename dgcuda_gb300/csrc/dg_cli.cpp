@@ -15,12 +15,20 @@
 //     --eq advection|euler|shallowwater|maxwell   (equation module)
 //     --problem NAME   (adv_sine, adv_linear, euler_vortex, euler_riemann4,
 //                       euler_supersonic, sw_hump, sw_test, maxwell_plane,
-//                       euler_cylinder, euler_lshock, euler_doublemach)
+//                       euler_cylinder, euler_lshock, euler_doublemach,
+//                       euler_airfoil, adv_squarehill, adv_rotatinghill,
+//                       adv_spin, maxwell_cmirror, maxwell_wscatter, euler_pulse)
+//     --reference-settings   start from the problem file's own settings
+//                      (limiter, time integrator, Mach, velocity); the
+//                      options below override them
 //     --scheme rk4|rk2|ssprk3   (time_integrator; default rk4)
 //     --limiter        (limiter = LIMITER)
 //     --cfl x          (default: 0.5 for rk4, 0.7 for rk2, 0.3 for ssprk3)
 //     --gamma g  --gravity g  --velocity ax,ay  --mu m  --eps e
 //     --prm a,b,...    problem parameters
+//     --field gxx,gxy,gyx,gyy  advection velocity (ax, ay) + grad (x, y)
+//     --series t0,a1,w1,f1,a2,w2,f2,...  euler_pulse inflow pressure
+//                      1 + sum a_k cos(w_k (t + t0) + f_k)
 //     -o DIR           output directory (default "output")
 //     --restart FILE   start from a checkpoint (state, bed and time)
 //     --checkpoint FILE  write a checkpoint at the end
@@ -55,7 +63,8 @@ void usage() {
       "          [--eq advection|euler|shallowwater|maxwell] [--problem NAME]\n"
       "          [--scheme rk4|rk2|ssprk3] [--limiter] [--cfl X] [--gamma G]\n"
       "          [--gravity G] [--velocity AX,AY] [--mu M] [--eps E] [--prm A,B,..]\n"
-      "          [-o DIR] [--restart FILE] [--checkpoint FILE]\n");
+      "          [--reference-settings] [--field GXX,GXY,GYX,GYY]\n"
+      "          [--series T0,A1,W1,F1,..] [-o DIR] [--restart FILE] [--checkpoint FILE]\n");
 }
 
 std::vector<double> parse_list(const char *s) {
@@ -103,12 +112,31 @@ int main(int argc, char **argv) {
   double endtime = -1, tol = 0, cfl = -1;
   std::string eq_name = "euler", problem = "none", scheme_name = "rk4", outdir = "output";
   std::string restart, checkpoint;
+  std::vector<double> field, series;
+  const char *pbs[] = {"none", "adv_sine", "adv_linear", "euler_vortex", "euler_riemann4",
+                       "euler_supersonic", "sw_hump", "sw_test", "maxwell_plane",
+                       "euler_cylinder", "euler_lshock", "euler_doublemach", "euler_airfoil",
+                       "adv_squarehill", "adv_rotatinghill", "adv_spin", "maxwell_cmirror",
+                       "maxwell_wscatter", "euler_pulse"};
+  const int npbs = (int)(sizeof pbs / sizeof pbs[0]);
   dg_params prm;
   dg_params_default(&prm);
   if (argc < 2) {
     usage();
     return 1;
   }
+  // the problem's own settings first, so that the options override them
+  for (int i = 1; i < argc - 1; i++)
+    if (!std::strcmp(argv[i], "--reference-settings")) {
+      int pb = -1, sc = DG_RK4;
+      for (int j = 1; j + 1 < argc - 1; j++)
+        if (!std::strcmp(argv[j], "--problem"))
+          for (int k = 0; k < npbs; k++)
+            if (!std::strcmp(argv[j + 1], pbs[k])) pb = k;
+      if (pb < 0 || dg_params_for_problem(&prm, pb, &sc) != DG_OK) { usage(); return 1; }
+      limiter = prm.limiter;
+      scheme_name = sc == DG_RK2 ? "rk2" : "rk4";
+    }
   for (int i = 1; i < argc; i++)
     if (!std::strcmp(argv[i], "-h")) {
       usage();
@@ -145,6 +173,14 @@ int main(int argc, char **argv) {
     else if (a == "--problem") problem = next();
     else if (a == "--scheme") scheme_name = next();
     else if (a == "--limiter") limiter = 1;
+    else if (a == "--reference-settings") continue;
+    else if (a == "--field") {
+      field = parse_list(next());
+      if (field.size() != 4) { usage(); return 1; }
+    } else if (a == "--series") {
+      series = parse_list(next());
+      if (series.size() % 3 != 1 || series.size() > 49) { usage(); return 1; }
+    }
     else if (a == "--cfl") cfl = std::atof(next());
     else if (a == "--gamma") prm.gamma = std::atof(next());
     else if (a == "--gravity") prm.gravity = std::atof(next());
@@ -174,11 +210,8 @@ int main(int argc, char **argv) {
   else if (eq_name == "shallowwater") eq = DG_SHALLOW_WATER;
   else if (eq_name == "maxwell") eq = DG_MAXWELL;
   else { usage(); return 1; }
-  const char *pbs[] = {"none", "adv_sine", "adv_linear", "euler_vortex", "euler_riemann4",
-                       "euler_supersonic", "sw_hump", "sw_test", "maxwell_plane",
-                       "euler_cylinder", "euler_lshock", "euler_doublemach"};
   prm.problem = -1;
-  for (int k = 0; k < 12; k++)
+  for (int k = 0; k < npbs; k++)
     if (problem == pbs[k]) prm.problem = k;
   if (prm.problem < 0) { usage(); return 1; }
   dg_scheme scheme;
@@ -200,6 +233,19 @@ int main(int argc, char **argv) {
   dg_mesh_get_arrays(mesh, V.data(), nullptr, nullptr, nullptr);
   dg_solver *s = nullptr;
   if (dg_solver_create(mesh, eq, p, &prm, 0, &s) != DG_OK) return fail("creating the solver");
+  if (!field.empty() && dg_set_velocity_field(s, prm.ax, prm.ay, field.data()) != DG_OK)
+    return fail("the velocity field");
+  if (!series.empty()) {
+    const int n = (int)(series.size() - 1) / 3;
+    std::vector<double> amp(n), omega(n), phase(n);
+    for (int k = 0; k < n; k++) {
+      amp[k] = series[1 + 3 * k];
+      omega[k] = series[2 + 3 * k];
+      phase[k] = series[3 + 3 * k];
+    }
+    if (dg_set_inflow_series(s, n, amp.data(), omega.data(), phase.data(), series[0]) != DG_OK)
+      return fail("the inflow series");
+  }
   if (dg_init(s) != DG_OK) return fail("initial conditions");
   int N = 0, np = 0;
   dg_solver_sizes(s, &N, &np, nullptr, nullptr);

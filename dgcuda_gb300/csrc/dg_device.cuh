@@ -38,7 +38,9 @@ struct Tab {
 enum Problem {
   PB_NONE = 0, PB_ADV_SINE = 1, PB_ADV_LINEAR = 2, PB_EULER_VORTEX = 3, PB_EULER_RIEMANN4 = 4,
   PB_EULER_SUPERSONIC = 5, PB_SW_HUMP = 6, PB_SW_TEST = 7, PB_MAXWELL_PLANE = 8,
-  PB_EULER_CYLINDER = 9, PB_EULER_LSHOCK = 10, PB_EULER_DOUBLEMACH = 11
+  PB_EULER_CYLINDER = 9, PB_EULER_LSHOCK = 10, PB_EULER_DOUBLEMACH = 11, PB_EULER_AIRFOIL = 12,
+  PB_ADV_SQUAREHILL = 13, PB_ADV_ROTATINGHILL = 14, PB_ADV_SPIN = 15, PB_MAXWELL_CMIRROR = 16,
+  PB_MAXWELL_WSCATTER = 17, PB_EULER_PULSE = 18
 };
 
 // double Mach reflection (euler/doublemach/doublemach.cu): the wall starts at
@@ -67,6 +69,34 @@ DG_HD void uniform_mach(const EqP &q, double M, double *U) {
 }
 
 constexpr double kPi = 3.141592653589793238462643383279502884;
+
+// a Gaussian hill A exp(-|x - x0|^2 / (2 r^2)) carried by the solid rotation
+// of angular speed w about the origin: the state at time t is the initial
+// hill at the point rotated back by w t (rotatinghill.cu:58-67, whose
+// inflow is this formula; spin.cu has the same form with its own hill)
+DG_HD double rotated_hill(double A, double x0, double y0, double r, double w, double x, double y,
+                          double t) {
+  const double c = cos(w * t), s = sin(w * t);
+  const double dx = fma(x, c, fma(y, s, -x0)), dy = fma(-x, s, fma(y, c, -y0));
+  return A * exp(-fma(dx, dx, dy * dy) / (2 * r * r));
+}
+// rotation speeds of the two rotating problems: each file's velocity field
+// (-2 PI y, 2 PI x) with its own PI (rotatinghill.cu:10, spin.cu:10)
+constexpr double kRotHill = 2 * 3.14159265358979323, kRotSpin = 2 * 3.14159;
+
+// the inflow pressure series of the tube and trumpet problems (tube.cu:52-97,
+// trumpet.cu: U_inflow): p(t) = 1 + sum_k amp_k cos(omega_k (t + t0) +
+// phase_k), rho = gamma p^(1/gamma), u = (p - 1) / gamma, v = 0
+DG_HD void pulse_state(const EqP &q, double t, double *U) {
+  double p = 1.0;
+  const double tt = t + q.ser_t0;
+  for (int k = 0; k < q.nser; k++) p += q.ser[k][0] * cos(fma(q.ser[k][1], tt, q.ser[k][2]));
+  const double rho = q.gamma * pow(p, 1. / q.gamma), u = (p - 1) / q.gamma;
+  U[0] = rho;
+  U[1] = u * rho;
+  U[2] = 0.;
+  U[3] = fma(0.5 * rho, u * u, p / (q.gamma - 1.));
+}
 
 // a product that is not fused into an FMA with a later add (same rounding in
 // every kernel instance that inlines the caller)
@@ -175,6 +205,29 @@ DG_HD void exact_state(const EqP &q, double *U, double x, double y, double t) {
       if (x < kDmX0 + (1. + 20. * t) / sqrt(3.)) dm_shock(q, U);
       else dm_rest(q, U);
       break;
+    case PB_EULER_AIRFOIL: {  // airfoil.cu:22-45: uniform flow at Mach P[0] (0: 0.98),
+                              // P[1] degrees (0: 5)
+      const double M = P[0] != 0 ? P[0] : 0.98, a = (P[1] != 0 ? P[1] : 5.) * (kPi / 180.);
+      U[0] = q.gamma;
+      U[1] = U[0] * M * cos(a);
+      U[2] = U[0] * M * sin(a);
+      U[3] = fma(0.5 * U[0], M * M, 1. / (q.gamma - 1.0));
+      break;
+    }
+    case PB_EULER_PULSE:  // U_inflow = U_outflow
+      pulse_state(q, t, U);
+      break;
+    case PB_ADV_SQUAREHILL: {  // squarehill.cu:22-30, translated by a t
+      const double xs = x - q.ax * t, ys = y - q.ay * t;
+      U[0] = (xs < -.2 && xs > -.8 && ys < .1 && ys > -.5) ? 1. : 0.;
+      break;
+    }
+    case PB_ADV_ROTATINGHILL:
+      U[0] = rotated_hill(5., 0.2, 0.0, 0.15, kRotHill, x, y, t);
+      break;
+    case PB_ADV_SPIN:  // spin.cu:22-30
+      U[0] = rotated_hill(1., 0.5, 0.5, 0.1, kRotSpin, x, y, t);
+      break;
     case PB_MAXWELL_PLANE: {  // plane TM wave along x
       double c = 1 / sqrt(q.mu * q.eps);
       double ez = sin(2 * kPi * (x - c * t));
@@ -188,6 +241,27 @@ DG_HD void exact_state(const EqP &q, double *U, double x, double y, double t) {
   }
 }
 
+// the inflow state (U_inflow): the exact state, except where a problem's
+// inflow differs from it
+DG_HD void inflow_state(const EqP &q, double *U, double x, double y, double t) {
+  switch (q.problem) {
+    case PB_ADV_SQUAREHILL:  // squarehill.cu:43-45
+    case PB_ADV_SPIN:        // spin.cu:43-46
+      U[0] = 0.;
+      return;
+    case PB_MAXWELL_CMIRROR:  // cmirror.cu:38-47: a half-period pulse of E_z
+      U[0] = U[1] = 0.;
+      U[2] = t <= 1. / 20 ? 2 * sin(20. * kPi * t) : 0.;
+      return;
+    case PB_MAXWELL_WSCATTER:  // wscatter.cu:38-50: a pulse through a slit |y| < 0.15
+      U[0] = U[1] = 0.;
+      U[2] = (y < .15 && y > -.15 && t < 0.5) ? sin(2. * kPi * t) : 0.;
+      return;
+    default:
+      exact_state(q, U, x, y, t);
+  }
+}
+
 // the initial state (U0): the exact state at t = 0, except where a problem's
 // initial data differ from its boundary data
 DG_HD void init_state(const EqP &q, double *U, double x, double y) {
@@ -195,6 +269,10 @@ DG_HD void init_state(const EqP &q, double *U, double x, double y) {
     const double angle = atan(y / (x - kDmX0));
     if (angle > 60. * kPi / 180 || x < kDmX0) dm_shock(q, U);
     else dm_rest(q, U);
+    return;
+  }
+  if (q.problem == PB_EULER_PULSE) {  // tube.cu:25-45: gas at rest, rho = gamma, p = 1
+    dm_rest(q, U);
     return;
   }
   exact_state(q, U, x, y, 0.0);
@@ -206,10 +284,29 @@ DG_HD void init_state(const EqP &q, double *U, double x, double y) {
 struct Advection {  // advection/advection.cu
   static constexpr int N = 1;
   static constexpr bool kBathymetry = false;
+  // the velocity may vary in space (q.field): fluxes then take the position
+  static constexpr bool kField = true;
   DG_HD static bool physical(const EqP &, const double *) { return true; }
   DG_HD static void flux(const EqP &q, const double *U, double *fx, double *fy) {
     fx[0] = q.ax * U[0];
     fy[0] = q.ay * U[0];
+  }
+  // get_velocity (advection.cu:12; rotatinghill.cu:37-40): the affine field
+  // a(x, y) = (ax, ay) + agrad (x, y)
+  DG_HD static void velocity(const EqP &q, double x, double y, double &vx, double &vy) {
+    vx = fma(q.agrad[0], x, fma(q.agrad[1], y, q.ax));
+    vy = fma(q.agrad[2], x, fma(q.agrad[3], y, q.ay));
+  }
+  // eval_flux with the velocity at the point (advection.cu:51-72)
+  DG_HD static void flux_at(double vx, double vy, const double *U, double *fx, double *fy) {
+    fx[0] = vx * U[0];
+    fy[0] = vy * U[0];
+  }
+  // upwind flux with the velocity at the point (advection.cu:94-116)
+  DG_HD static void riemann_at(double vx, double vy, const double *UL, const double *UR,
+                               double nx, double ny, double *F) {
+    double an = fma(nx, vx, ny * vy);
+    F[0] = an > 0 ? an * UL[0] : an * UR[0];
   }
   // upwind flux (riemann_solver_upwind, advection.cu:94-116)
   // riemann_raw(..) * kRawScale is the numerical flux; face kernels fold the
@@ -221,7 +318,10 @@ struct Advection {  // advection/advection.cu
     F[0] = an > 0 ? an * UL[0] : an * UR[0];
   }
   DG_HD static double mean_speed(const EqP &q, const double *) {
-    return sqrt(fma(q.ax, q.ax, q.ay * q.ay));
+    // a field: the largest speed over the elements, each taken at its middle
+    // quadrature point (eval_global_lambda, advection.cu:157-183), which
+    // does not change in time and is found once on the host
+    return q.field ? q.amax : sqrt(fma(q.ax, q.ax, q.ay * q.ay));
   }
   DG_HD static void reflect(const EqP &, const double *, double *UR, double, double, double,
                             double) {
@@ -233,6 +333,7 @@ struct Advection {  // advection/advection.cu
 struct Euler {  // euler/euler.cu
   static constexpr int N = 4;
   static constexpr bool kBathymetry = false;
+  static constexpr bool kField = false;
   // rho >= 0 and p >= 0 (is_physical, euler.cu:76-86); with rho > 0,
   // p < 0 <=> 2 rho E < |rho u|^2, which needs no FP64 division
   DG_HD static bool physical(const EqP &, const double *U) {
@@ -309,6 +410,7 @@ struct Euler {  // euler/euler.cu
 struct ShallowWater {  // shallowwater/shallowwater.cu (g is a parameter here)
   static constexpr int N = 3;
   static constexpr bool kBathymetry = true;  // optional bed b(x, y): source -g h grad b
+  static constexpr bool kField = false;
   DG_HD static bool physical(const EqP &, const double *U) { return U[0] >= 0.; }
   DG_HD static void flux(const EqP &q, const double *U, double *fx, double *fy) {
     double ih = rcp(U[0]);
@@ -350,6 +452,7 @@ struct ShallowWater {  // shallowwater/shallowwater.cu (g is a parameter here)
 struct Maxwell {  // maxwells/maxwells.cu, U = (Hx, Hy, Ez)
   static constexpr int N = 3;
   static constexpr bool kBathymetry = false;
+  static constexpr bool kField = false;
   DG_HD static bool physical(const EqP &, const double *) { return true; }
   DG_HD static void flux(const EqP &q, const double *U, double *fx, double *fy) {
     double imu = 1. / q.mu, ieps = 1. / q.eps;
@@ -372,10 +475,11 @@ struct Maxwell {  // maxwells/maxwells.cu, U = (Hx, Hy, Ez)
   DG_HD static double mean_speed(const EqP &q, const double *) { return fabs(1. / sqrt(q.eps * q.mu)); }
   DG_HD static void reflect(const EqP &, const double *UL, double *UR, double, double, double nx,
                             double ny) {  // maxwells/cmirror/cmirror.cu:63-77
+    // E_z kept; H: the normal component kept, the tangential one reversed
     double dot = fma(UL[0], nx, UL[1] * ny);
     UR[2] = UL[2];
-    UR[0] = fma(-2 * dot, nx, UL[0]);
-    UR[1] = fma(-2 * dot, ny, UL[1]);
+    UR[0] = fma(2 * dot, nx, -UL[0]);
+    UR[1] = fma(2 * dot, ny, -UL[1]);
   }
   static constexpr bool outflow_uses_exact = false;
 };
@@ -387,8 +491,8 @@ DG_HD void ghost_state(const EqP &q, int code, const double *UL, double *UR, dou
   double G[4] = {0, 0, 0, 0};
   if (code == -4) {  // transmissive (new)
     for (int n = 0; n < Eq::N; n++) G[n] = UL[n];
-  } else if (code == -3) {  // inflow = the problem's exact state
-    exact_state(q, G, x, y, t);
+  } else if (code == -3) {  // inflow
+    inflow_state(q, G, x, y, t);
   } else if (code == -2) {  // outflow
     if (Eq::outflow_uses_exact) exact_state(q, G, x, y, t);
   } else {  // reflect

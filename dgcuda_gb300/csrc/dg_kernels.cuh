@@ -102,10 +102,11 @@ struct FaceArgs {
   const double *T;
   const int4 *side;
   const double *sgeo, *bxy;
+  const double *vtx;  // element vertices (rows of Kp): edge-point positions of a velocity field
   double *Fh;
   const double *tptr, *dtp;
   double tcoef;
-  int S, Sb;
+  int S, Sb, Kp;
 };
 
 template <class Eq, int P>
@@ -127,7 +128,22 @@ __device__ __forceinline__ void face_body(const Tab<P> &tab, const EqP &q, const
         UL[n] = TL[j * N + n];
         UR[n] = TR[(N1 - 1 - j) * N + n];
       }
-      Eq::riemann_raw(q, UL, UR, nx, ny, Fn);
+      if constexpr (Eq::kField) {
+        if (q.field) {  // the velocity at the edge point, on the left face
+          const int va = sd.z, vb = sd.z == 2 ? 0 : sd.z + 1;
+          const size_t Kp = a.Kp;
+          const double xa = a.vtx[2 * va * Kp + sd.x], ya = a.vtx[(2 * va + 1) * Kp + sd.x];
+          const double xb = a.vtx[2 * vb * Kp + sd.x], yb = a.vtx[(2 * vb + 1) * Kp + sd.x];
+          const double r = 0.5 + 0.5 * tab.t1[j];
+          double vx, vy;
+          Eq::velocity(q, fma(r, xb - xa, xa), fma(r, yb - ya, ya), vx, vy);
+          Eq::riemann_at(vx, vy, UL, UR, nx, ny, Fn);
+        } else {
+          Eq::riemann_raw(q, UL, UR, nx, ny, Fn);
+        }
+      } else {
+        Eq::riemann_raw(q, UL, UR, nx, ny, Fn);
+      }
       const double sc = hl * tab.w1[j] * Eq::kRawScale;  // exact: a power of two
 #pragma unroll
       for (int n = 0; n < N; n++) F[j * N + n] = Fn[n] * sc;
@@ -142,8 +158,19 @@ __device__ __forceinline__ void face_body(const Tab<P> &tab, const EqP &q, const
 #pragma unroll
       for (int n = 0; n < N; n++) UL[n] = TL[j * N + n];
       const double r = 0.5 + 0.5 * tab.t1[j];
-      ghost_state<Eq>(q, sd.y, UL, UR, fma(r, xb - xa, xa), fma(r, yb - ya, ya), t, nx, ny);
-      Eq::riemann_raw(q, UL, UR, nx, ny, Fn);
+      const double px = fma(r, xb - xa, xa), py = fma(r, yb - ya, ya);
+      ghost_state<Eq>(q, sd.y, UL, UR, px, py, t, nx, ny);
+      if constexpr (Eq::kField) {
+        if (q.field) {
+          double vx, vy;
+          Eq::velocity(q, px, py, vx, vy);
+          Eq::riemann_at(vx, vy, UL, UR, nx, ny, Fn);
+        } else {
+          Eq::riemann_raw(q, UL, UR, nx, ny, Fn);
+        }
+      } else {
+        Eq::riemann_raw(q, UL, UR, nx, ny, Fn);
+      }
       const double sc = hl * tab.w1[j] * Eq::kRawScale;  // exact: a power of two
 #pragma unroll
       for (int n = 0; n < N; n++) F[j * N + n] = Fn[n] * sc;
@@ -166,7 +193,8 @@ template <class Eq, int P>
 __device__ __forceinline__ bool volume(const Tab<P> &tab, const EqP &q,
                                        const double (&c)[Eq::N][Tab<P>::NP],
                                        double (&acc)[Eq::N][Tab<P>::NP], double xr, double yr,
-                                       double xs, double ys, const double *bz) {
+                                       double xs, double ys, const double *bz, double x1 = 0.0,
+                                       double y1 = 0.0) {
   constexpr int N = Eq::N, NP = Tab<P>::NP, NQ = Tab<P>::NQ;
   bool ok = true;
 #pragma unroll
@@ -180,7 +208,16 @@ __device__ __forceinline__ bool volume(const Tab<P> &tab, const EqP &q,
       U[n] = a;
     }
     ok &= Eq::physical(q, U);
-    Eq::flux(q, U, fx, fy);
+    if constexpr (Eq::kField) {
+      // velocity at the point x = x1 + xr r + xs s (get_coordinates_2d, :231-235)
+      double vx = q.ax, vy = q.ay;
+      if (q.field)
+        Eq::velocity(q, fma(xr, tab.r[k], fma(xs, tab.s[k], x1)),
+                     fma(yr, tab.r[k], fma(ys, tab.s[k], y1)), vx, vy);
+      Eq::flux_at(vx, vy, U, fx, fy);
+    } else {
+      Eq::flux(q, U, fx, fy);
+    }
     // [fx fy] [y_s -y_r; -x_s x_r] folded once per point (eval_volume :1066-1074)
 #pragma unroll
     for (int n = 0; n < N; n++) {
@@ -222,6 +259,7 @@ struct ElemArgs {
   const double *geo;        // metric
   const double *dtp;        // time step
   const double *bathy;      // bed modes [mode][Kp] (shallow water) or null
+  const double *vtx;        // element vertices (rows of Kp): positions for a velocity field
   double *T;                // traces of out (TR)
   double ca, cb, cc;
   int K, Kp, check;
@@ -255,7 +293,14 @@ __device__ __forceinline__ void element_body(const Tab<P> &tab, const EqP &q, co
       bz[i] = has_b ? a.bathy[(size_t)i * Kp + e] : 0.0;
   }
   const double *bzp = has_b ? bz : nullptr;
-  if (!volume<Eq, P>(tab, q, c, acc, xr, yr, xs, ys, bzp)) {
+  double x1 = 0.0, y1 = 0.0;
+  if constexpr (Eq::kField) {
+    if (q.field) {
+      x1 = a.vtx[e];
+      y1 = a.vtx[(size_t)Kp + e];
+    }
+  }
+  if (!volume<Eq, P>(tab, q, c, acc, xr, yr, xs, ys, bzp, x1, y1)) {
     // non-physical volume value: the element's mean replaces it everywhere
 #pragma unroll
     for (int n = 0; n < N; n++)
@@ -264,7 +309,7 @@ __device__ __forceinline__ void element_body(const Tab<P> &tab, const EqP &q, co
         acc[n][i] = 0.0;
         if (i > 0) c[n][i] = 0.0;
       }
-    volume<Eq, P>(tab, q, c, acc, xr, yr, xs, ys, bzp);
+    volume<Eq, P>(tab, q, c, acc, xr, yr, xs, ys, bzp, x1, y1);
     if (us != out)
 #pragma unroll
       for (int n = 0; n < N; n++)
@@ -692,6 +737,7 @@ __device__ __forceinline__ ElemArgs batch_elem_args(const BatchProb &pr, int sta
   a.geo = pr.geo;
   a.dtp = &pr.ds->dt;
   a.bathy = pr.bathy;
+  a.vtx = pr.vtx;
   a.T = pr.T;
   a.ca = stage == 0 ? 0.0 : stage == 1 ? 0.75 : 1.0 / 3.0;
   a.cb = stage == 0 ? 1.0 : stage == 1 ? 0.25 : 2.0 / 3.0;
@@ -732,12 +778,14 @@ __global__ void __launch_bounds__(kMaxBlock)
   a.side = pr.side;
   a.sgeo = pr.sgeo;
   a.bxy = pr.bxy;
+  a.vtx = pr.vtx;
   a.Fh = pr.Fh;
   a.tptr = &pr.ds->t;
   a.dtp = &pr.ds->dt;
   a.tcoef = tcoef;
   a.S = pr.S;
   a.Sb = pr.Sb;
+  a.Kp = pr.Kp;
   switch (pr.p) {
     case 1: face_body<Eq, 1>(tb.t1, pr.q, a, s); break;
     case 2: face_body<Eq, 2>(tb.t2, pr.q, a, s); break;
@@ -823,6 +871,7 @@ struct Launch {
     a.geo = c.m.geo;
     a.dtp = dtp;
     a.bathy = c.m.bathy;
+    a.vtx = c.m.vtx;
     a.T = T;
     a.ca = ca;
     a.cb = cb;
@@ -845,12 +894,14 @@ struct Launch {
     a.side = c.m.side;
     a.sgeo = c.m.sgeo;
     a.bxy = c.m.bxy;
+    a.vtx = c.m.vtx;
     a.Fh = c.Fh;
     a.tptr = t;
     a.dtp = &c.ds->dt;
     a.tcoef = tcoef;
     a.S = c.m.S;
     a.Sb = c.m.Sb;
+    a.Kp = c.m.Kp;
     DG_DISPATCH_P((k_face<Eq, P><<<nblk(c.m.S, c.blk), c.blk, 0, c.st>>>(tab<P>(c), *c.q, a)));
   }
   static void element(const Ctx &c, double *us, const double *un, double *out, double ca,

@@ -9,10 +9,18 @@
 namespace dg {
 
 // equation / problem parameters (kernel parameter)
+constexpr int kMaxSeries = 16;  // terms of an inflow pressure series
 struct EqP {
   double gamma, g, ax, ay, mu, eps;
-  int problem, pad;
+  int problem;
+  int field;        // 1: advection velocity a(x, y) = (ax, ay) + agrad (x, y)
   double prm[8];
+  double agrad[4];  // d a_x/dx, d a_x/dy, d a_y/dx, d a_y/dy
+  double amax;      // field: the largest element speed (the CFL wave speed)
+  // inflow pressure series p(t) = 1 + sum_k amp_k cos(omega_k (t + t0) + phase_k)
+  double ser_t0;
+  double ser[kMaxSeries][3];  // amp, omega, phase
+  int nser, pad;
 };
 
 // Device-resident mesh in internal (space-filling-curve) element order.
@@ -69,6 +77,7 @@ struct BatchProb {
   const int *esd, *nbr;
   const int4 *side;
   const double *sgeo, *bxy, *bathy;
+  const double *vtx;
   DevScalars *ds;
   EqP q;
 };

@@ -43,6 +43,61 @@ extern "C" void dg_params_default(dg_params *p) {
   p->cfl = 0.3;
 }
 
+// the reference problem's own settings: each problem file's limiter and
+// time_integrator globals, its GAMMA / MACH / ALPHA defines and its
+// get_velocity (e.g. airfoil.cu:9-14, squarehill.cu:11-12, spin.cu:11-12)
+extern "C" dg_status dg_params_for_problem(dg_params *p, int problem, int *scheme) {
+  if (!p) return dg::fail(DG_BAD_ARG, "null argument");
+  if (problem < DG_PB_NONE || problem > DG_PB_EULER_PULSE)
+    return dg::fail(DG_BAD_ARG, "unknown problem");
+  dg_params_default(p);
+  p->problem = problem;
+  int sc = DG_RK4;
+  switch (problem) {
+    case DG_PB_ADV_LINEAR:  // exact.cu:11-12, 34-37
+      p->ax = p->ay = 1.0;
+      p->limiter = 1;
+      break;
+    case DG_PB_ADV_SQUAREHILL:  // squarehill.cu:11-12, 35-38
+      p->ax = 1.0;
+      p->ay = 0.0;
+      p->limiter = 1;
+      break;
+    case DG_PB_ADV_ROTATINGHILL:  // the rotation is set by the problem
+      p->ax = p->ay = 0.0;
+      break;
+    case DG_PB_ADV_SPIN:  // spin.cu:11-12
+      p->ax = p->ay = 0.0;
+      sc = DG_RK2;
+      break;
+    case DG_PB_EULER_SUPERSONIC:  // supersonic.cu:10-14
+      p->limiter = 1;
+      break;
+    case DG_PB_EULER_CYLINDER:  // cylinder.cu:10
+      p->prm[0] = 0.38;
+      break;
+    case DG_PB_EULER_LSHOCK:  // lshock.cu:10
+      p->prm[0] = 2.0;
+      break;
+    case DG_PB_EULER_DOUBLEMACH:  // doublemach.cu:18-19
+      p->limiter = 1;
+      sc = DG_RK2;
+      break;
+    case DG_PB_EULER_AIRFOIL:  // airfoil.cu:10-14
+      p->prm[0] = 0.98;
+      p->prm[1] = 5.0;
+      p->limiter = 1;
+      break;
+    case DG_PB_SW_TEST:  // shallowwater.cu:7 hard-codes g = 9.8
+      p->gravity = 9.8;
+      break;
+    default:
+      break;
+  }
+  if (scheme) *scheme = sc;
+  return DG_OK;
+}
+
 namespace dg {
 
 dg_status validate_mesh(const dg_mesh &m) {

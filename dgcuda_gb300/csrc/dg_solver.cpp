@@ -237,6 +237,27 @@ dg_status ensure_rk_buffers(dg_solver *s) {
   return DG_OK;
 }
 
+// the CFL wave speed of an advection velocity field: the largest speed over
+// the elements, each taken at its middle quadrature point x = x1 + (x2 - x1)
+// r + (x3 - x1) s (eval_global_lambda, advection.cu:157-183); the field does
+// not change in time, so this is found once
+static void field_refresh(dg_solver *s) {
+  dg::EqP &q = s->q;
+  q.field = (q.agrad[0] != 0 || q.agrad[1] != 0 || q.agrad[2] != 0 || q.agrad[3] != 0) ? 1 : 0;
+  q.amax = 0.0;
+  if (!q.field) return;
+  const int k = s->tables.n_q / 2;
+  const double r = s->tables.r[k], sv = s->tables.s[k];
+  for (int e = 0; e < s->K; e++) {
+    const double *v = &s->mesh_v[(size_t)6 * e];
+    const double x = std::fma(v[2] - v[0], r, std::fma(v[4] - v[0], sv, v[0]));
+    const double y = std::fma(v[3] - v[1], r, std::fma(v[5] - v[1], sv, v[1]));
+    const double vx = std::fma(q.agrad[0], x, std::fma(q.agrad[1], y, q.ax));
+    const double vy = std::fma(q.agrad[2], x, std::fma(q.agrad[3], y, q.ay));
+    q.amax = std::max(q.amax, std::sqrt(std::fma(vx, vx, vy * vy)));
+  }
+}
+
 void drop_graphs(dg_solver *s) {
   for (auto &g : s->graphs) cudaGraphExecDestroy(g.second);
   s->graphs.clear();
@@ -402,7 +423,7 @@ extern "C" dg_status dg_solver_create(const dg_mesh *mesh, dg_equation eq, int p
   dg_params P;
   if (prm) P = *prm;
   else dg_params_default(&P);
-  if (P.problem < 0 || P.problem > DG_PB_EULER_DOUBLEMACH) return fail(DG_BAD_ARG, "unknown problem");
+  if (P.problem < 0 || P.problem > DG_PB_EULER_PULSE) return fail(DG_BAD_ARG, "unknown problem");
   if (!(P.cfl > 0)) return fail(DG_BAD_ARG, "cfl must be positive");
   if (eq == DG_EULER && !(P.gamma > 1)) return fail(DG_BAD_ARG, "gamma must be > 1");
   if (eq == DG_SHALLOW_WATER && !(P.gravity > 0)) return fail(DG_BAD_ARG, "gravity must be > 0");
@@ -432,6 +453,13 @@ extern "C" dg_status dg_solver_create(const dg_mesh *mesh, dg_equation eq, int p
   s->q.eps = P.eps;
   s->q.problem = P.problem;
   for (int i = 0; i < 8; i++) s->q.prm[i] = P.prm[i];
+  if (P.problem == DG_PB_ADV_ROTATINGHILL || P.problem == DG_PB_ADV_SPIN) {
+    // the solid rotation (-w y, w x) of rotatinghill.cu:37-40 / spin.cu:37-40
+    const double w = P.problem == DG_PB_ADV_SPIN ? dg::kRotSpin : dg::kRotHill;
+    s->q.ax = s->q.ay = 0.0;
+    s->q.agrad[1] = -w;
+    s->q.agrad[2] = w;
+  }
   s->tables = DG_TABLES[p];
   s->tabimg.resize(dg::tab_bytes(p));
   dg::build_tab(p, s->tables, s->tabimg.data());
@@ -504,6 +532,7 @@ extern "C" dg_status dg_solver_create(const dg_mesh *mesh, dg_equation eq, int p
   s->mesh_v.resize((size_t)6 * K);
   for (int o = 0; o < K; o++)
     for (int k = 0; k < 6; k++) s->mesh_v[(size_t)6 * o + k] = mesh->V[k][o];
+  field_refresh(s);
   // ---- side arrays ----
   std::vector<int4> side(S);
   std::vector<double> sgeo((size_t)3 * S), bxy((size_t)4 * std::max(Sb, 1));
@@ -659,6 +688,7 @@ extern "C" dg_status dg_solver_set_tables(dg_solver *s, int n_q, int n_1, const 
         return fail(DG_BAD_ARG, "basis function 0 must take one value on every edge point");
   s->tables = t;
   dg::build_tab(s->p, s->tables, s->tabimg.data());
+  field_refresh(s);
   drop_graphs(s);
   {
     dg_status ozs = oz_refresh(s);
@@ -1131,6 +1161,7 @@ extern "C" dg_status dg_batch_create(int n, dg_solver *const *members, dg_batch 
     q.sgeo = s->m.sgeo;
     q.bxy = s->m.bxy;
     q.bathy = s->m.bathy;
+    q.vtx = s->m.vtx;
     q.ds = s->ds;
     q.q = s->q;
   }
@@ -1810,5 +1841,59 @@ extern "C" dg_status dg_set_tensor_contractions(dg_solver *s, int on) {
 extern "C" dg_status dg_get_tensor_contractions(dg_solver *s, int *on) {
   if (!s || !on) return fail(DG_BAD_ARG, "null argument");
   *on = s->ctx.oz != nullptr;
+  return DG_OK;
+}
+
+// advection velocity a(x, y) = (ax, ay) + grad (x, y): the reference's
+// get_velocity (advection.cu:12) for fields affine in space, which covers
+// every reference problem (constant in exact.cu and squarehill.cu, a solid
+// rotation in rotatinghill.cu and spin.cu)
+extern "C" dg_status dg_set_velocity_field(dg_solver *s, double ax, double ay,
+                                           const double *grad) {
+  if (!s) return fail(DG_BAD_ARG, "null solver");
+  if (s->eq != DG_ADVECTION) return fail(DG_UNSUPPORTED, "a velocity field is for advection");
+  if (!std::isfinite(ax) || !std::isfinite(ay)) return fail(DG_BAD_ARG, "velocity not finite");
+  for (int i = 0; grad && i < 4; i++)
+    if (!std::isfinite(grad[i])) return fail(DG_BAD_ARG, "velocity gradient not finite");
+  CK(cudaSetDevice(s->device));
+  CK(cudaStreamSynchronize(s->st));
+  s->q.ax = ax;
+  s->q.ay = ay;
+  for (int i = 0; i < 4; i++) s->q.agrad[i] = grad ? grad[i] : 0.0;
+  field_refresh(s);
+  drop_graphs(s);
+  return DG_OK;
+}
+
+extern "C" dg_status dg_get_velocity_field(const dg_solver *s, double out[7]) {
+  if (!s || !out) return fail(DG_BAD_ARG, "null argument");
+  out[0] = s->q.ax;
+  out[1] = s->q.ay;
+  for (int i = 0; i < 4; i++) out[2 + i] = s->q.agrad[i];
+  out[6] = s->q.field ? s->q.amax : std::sqrt(std::fma(s->q.ax, s->q.ax, s->q.ay * s->q.ay));
+  return DG_OK;
+}
+
+// inflow pressure series of DG_PB_EULER_PULSE (the tube and trumpet problems'
+// U_inflow, tube.cu:52-97): p(t) = 1 + sum_k amp_k cos(omega_k (t + t0) + phase_k)
+extern "C" dg_status dg_set_inflow_series(dg_solver *s, int n, const double *amp,
+                                          const double *omega, const double *phase, double t0) {
+  if (!s) return fail(DG_BAD_ARG, "null solver");
+  if (n < 0 || n > dg::kMaxSeries) return fail(DG_BAD_ARG, "the series has 0..16 terms");
+  if (n > 0 && (!amp || !omega || !phase)) return fail(DG_BAD_ARG, "null argument");
+  if (!std::isfinite(t0)) return fail(DG_BAD_ARG, "t0 not finite");
+  for (int k = 0; k < n; k++)
+    if (!std::isfinite(amp[k]) || !std::isfinite(omega[k]) || !std::isfinite(phase[k]))
+      return fail(DG_BAD_ARG, "series coefficient not finite");
+  CK(cudaSetDevice(s->device));
+  CK(cudaStreamSynchronize(s->st));
+  s->q.nser = n;
+  s->q.ser_t0 = t0;
+  for (int k = 0; k < dg::kMaxSeries; k++) {
+    s->q.ser[k][0] = k < n ? amp[k] : 0.0;
+    s->q.ser[k][1] = k < n ? omega[k] : 0.0;
+    s->q.ser[k][2] = k < n ? phase[k] : 0.0;
+  }
+  drop_graphs(s);
   return DG_OK;
 }

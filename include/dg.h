@@ -58,8 +58,22 @@ typedef enum {
   DG_PB_EULER_CYLINDER = 9, /* uniform flow past a cylinder at the origin (euler/cylinder):
                                prm[0] Mach (0: 0.38); walls are the circle through the point */
   DG_PB_EULER_LSHOCK = 10,  /* uniform flow with slip walls (euler/lshock): prm[0] Mach (0: 2) */
-  DG_PB_EULER_DOUBLEMACH = 11 /* double Mach reflection (euler/doublemach): a Mach 10 shock
+  DG_PB_EULER_DOUBLEMACH = 11, /* double Mach reflection (euler/doublemach): a Mach 10 shock
                                at 60 degrees; the wall reflects from x = 1/6 on */
+  DG_PB_EULER_AIRFOIL = 12, /* uniform flow (euler/airfoil): prm[0] Mach (0: 0.98), prm[1]
+                               angle of attack in degrees (0: 5) */
+  DG_PB_ADV_SQUAREHILL = 13, /* box (-0.8,-0.2) x (-0.5,0.1) translated by a t
+                               (advection/rotatinghill/squarehill.cu); inflow 0 */
+  DG_PB_ADV_ROTATINGHILL = 14, /* Gaussian hill carried by the rotation (-2 pi y, 2 pi x)
+                               (advection/rotatinghill); the problem sets that velocity */
+  DG_PB_ADV_SPIN = 15,      /* advection/spin: its hill and rotation (with pi = 3.14159);
+                               inflow 0 */
+  DG_PB_MAXWELL_CMIRROR = 16, /* maxwells/cmirror: rest; inflow E_z = 2 sin(20 pi t) for
+                               t <= 1/20 */
+  DG_PB_MAXWELL_WSCATTER = 17, /* maxwells/wscatter: rest; inflow E_z = sin(2 pi t) through
+                               |y| < 0.15 for t < 1/2 */
+  DG_PB_EULER_PULSE = 18    /* euler/tube and euler/trumpet: gas at rest; inflow and outflow
+                               the pressure series of dg_set_inflow_series */
 } dg_problem;
 
 /* boundary codes in the .pmsh right-element column (genmesh.py:166-174) */
@@ -87,6 +101,10 @@ const char *dg_last_error(void);
 /* fills *p with the defaults: gamma 1.4, g 9.81, a = (1, 0.5), mu = eps = 1,
  * cfl 0.3, limiter off, problem DG_PB_NONE */
 void dg_params_default(dg_params *p);
+/* the defaults, then the reference problem's own settings (its limiter,
+ * Mach number, angle, velocity, g); *scheme (may be NULL) receives its time
+ * integrator (DG_RK4 or DG_RK2), the problem file's time_integrator global */
+dg_status dg_params_for_problem(dg_params *p, int problem, int *scheme);
 
 /* ---- meshes (host only; no GPU needed) ---------------------------------
  * replaces read_mesh (main.cu:205-277) and genmesh.py's .pmsh writer
@@ -184,6 +202,24 @@ dg_status dg_eval_vertices(dg_solver *s, int var, double *uv);
 #define DG_VIEW_EXACT 1
 #define DG_VIEW_ERROR 2
 dg_status dg_eval_vertices_view(dg_solver *s, int var, int view, double t, double *uv);
+
+/* advection velocity a(x, y) = (ax, ay) + grad (x, y), grad = {d a_x/dx,
+ * d a_x/dy, d a_y/dx, d a_y/dy} (NULL: constant).  Replaces the problem's
+ * get_velocity (advection.cu:12, rotatinghill.cu:37-40): the flux, the upwind
+ * flux and the CFL wave speed take it at each point, the wave speed of an
+ * element at its middle quadrature point (eval_global_lambda,
+ * advection.cu:157-183).  Advection only (else DG_UNSUPPORTED).  The
+ * rotating problems set their rotation when the solver is created. */
+dg_status dg_set_velocity_field(dg_solver *s, double ax, double ay, const double *grad);
+/* out[0..1] = (ax, ay), out[2..5] = grad, out[6] = the CFL wave speed */
+dg_status dg_get_velocity_field(const dg_solver *s, double out[7]);
+/* inflow pressure series of DG_PB_EULER_PULSE (tube.cu:52-97): p(t) = 1 +
+ * sum_k amp[k] cos(omega[k] (t + t0) + phase[k]), k < n <= 16; the ghost
+ * state is rho = gamma p^(1/gamma), u = (p - 1) / gamma, v = 0.  The tube and
+ * trumpet problems are this with their own coefficient tables (amp = twice
+ * each printed amplitude, omega = 2 PI times each frequency, t0 = 0.9197). */
+dg_status dg_set_inflow_series(dg_solver *s, int n, const double *amp, const double *omega,
+                               const double *phase, double t0);
 
 /* The fused SSP-RK3 element stage computes its basis contractions (area
  * values, volume and surface projections, next-stage traces) either with

@@ -56,12 +56,20 @@ enum { EQ_ADV = 0, EQ_EULER = 1, EQ_SW = 2, EQ_MAXWELL = 3 };
 enum {
   PB_NONE = 0, PB_ADV_SINE = 1, PB_ADV_LINEAR = 2, PB_EULER_VORTEX = 3, PB_EULER_RIEMANN4 = 4,
   PB_EULER_SUPERSONIC = 5, PB_SW_HUMP = 6, PB_SW_TEST = 7, PB_MAXWELL_PLANE = 8,
-  PB_EULER_CYLINDER = 9, PB_EULER_LSHOCK = 10, PB_EULER_DOUBLEMACH = 11
+  PB_EULER_CYLINDER = 9, PB_EULER_LSHOCK = 10, PB_EULER_DOUBLEMACH = 11, PB_EULER_AIRFOIL = 12,
+  PB_ADV_SQUAREHILL = 13, PB_ADV_ROTATINGHILL = 14, PB_ADV_SPIN = 15, PB_MAXWELL_CMIRROR = 16,
+  PB_MAXWELL_WSCATTER = 17, PB_EULER_PULSE = 18
 };
+#define NSER 16
 
 typedef struct or_solver {
   int eq, p, N, np, nq, n1, K, S, problem;
   double gamma, g, ax, ay, mu, eps, prm[8];
+  /* advection velocity a = (ax, ay) + agrad (x, y) (extension of a constant
+   * get_velocity to affine fields); inflow pressure series (tube.cu:52-97) */
+  double agrad[4];
+  int nser;
+  double ser_t0, ser[NSER][3];
   /* tables */
   double r[NQM], s[NQM], w[NQM], t1[N1M], w1[N1M];
   double B[NQM][NPM], GR[NQM][NPM], GS[NQM][NPM], E[3][N1M][NPM], VT[3][NPM];
@@ -208,6 +216,28 @@ static void uniform_mach(const or_solver *o, double M, double *U) {
   U[3] = 0.5 * U[0] * M * M + 1. / (o->gamma - 1.0);
 }
 
+/* Gaussian hill carried by the rotation of speed w about the origin: the
+ * initial hill at the point rotated back by w t (rotatinghill.cu:58-67) */
+#define ROT_HILL (2 * 3.14159265358979323) /* rotatinghill.cu:10 */
+#define ROT_SPIN (2 * 3.14159)             /* spin.cu:10 */
+static double rotated_hill(double A, double x0, double y0, double r, double w, double x, double y,
+                           double t) {
+  double c = cos(w * t), s = sin(w * t);
+  double dx = x * c + y * s - x0, dy = -x * s + y * c - y0;
+  return A * exp(-(dx * dx + dy * dy) / (2 * r * r));
+}
+
+/* inflow of the tube / trumpet problems (tube.cu:52-97) */
+static void pulse_state(const or_solver *o, double t, double *U) {
+  double p = 1.0, tt = t + o->ser_t0;
+  for (int k = 0; k < o->nser; k++) p += o->ser[k][0] * cos(o->ser[k][1] * tt + o->ser[k][2]);
+  double rho = o->gamma * pow(p, 1. / o->gamma), u = (p - 1) / o->gamma;
+  U[0] = rho;
+  U[1] = u * rho;
+  U[2] = 0.;
+  U[3] = 0.5 * rho * u * u + p / (o->gamma - 1.);
+}
+
 static void exact_state(const or_solver *o, double *U, double x, double y, double t) {
   const double *P = o->prm;
   switch (o->problem) {
@@ -284,6 +314,28 @@ static void exact_state(const or_solver *o, double *U, double x, double y, doubl
       if (x < DM_X0 + (1. + 20. * t) / sqrt(3.)) dm_shock(o, U);
       else dm_rest(o, U);
       break;
+    case PB_EULER_AIRFOIL: { /* airfoil.cu:22-45 */
+      double M = P[0] != 0 ? P[0] : 0.98, a = (P[1] != 0 ? P[1] : 5.) * (M_PI / 180.);
+      U[0] = o->gamma;
+      U[1] = U[0] * M * cos(a);
+      U[2] = U[0] * M * sin(a);
+      U[3] = 0.5 * U[0] * M * M + 1. / (o->gamma - 1.0);
+      break;
+    }
+    case PB_EULER_PULSE: /* tube.cu:52-97: U_inflow = U_outflow */
+      pulse_state(o, t, U);
+      break;
+    case PB_ADV_SQUAREHILL: { /* squarehill.cu:22-30, translated */
+      double xs = x - o->ax * t, ys = y - o->ay * t;
+      U[0] = (xs < -.2 && xs > -.8 && ys < .1 && ys > -.5) ? 1. : 0.;
+      break;
+    }
+    case PB_ADV_ROTATINGHILL: /* rotatinghill.cu:22-30, 58-67 */
+      U[0] = rotated_hill(5., 0.2, 0.0, 0.15, ROT_HILL, x, y, t);
+      break;
+    case PB_ADV_SPIN: /* spin.cu:22-30 */
+      U[0] = rotated_hill(1., 0.5, 0.5, 0.1, ROT_SPIN, x, y, t);
+      break;
     case PB_MAXWELL_PLANE: {
       double c = 1 / sqrt(o->mu * o->eps);
       double ez = sin(2 * M_PI * (x - c * t));
@@ -306,7 +358,31 @@ static void init_state(const or_solver *o, double *U, double x, double y) {
     else dm_rest(o, U);
     return;
   }
+  if (o->problem == PB_EULER_PULSE) { /* tube.cu:25-45: at rest */
+    dm_rest(o, U);
+    return;
+  }
   exact_state(o, U, x, y, 0.0);
+}
+
+/* U_inflow: the exact state except where a problem's inflow differs */
+static void inflow_state(const or_solver *o, double *U, double x, double y, double t) {
+  switch (o->problem) {
+    case PB_ADV_SQUAREHILL: /* squarehill.cu:43-45 */
+    case PB_ADV_SPIN:       /* spin.cu:43-46 */
+      U[0] = 0.;
+      return;
+    case PB_MAXWELL_CMIRROR: /* cmirror.cu:38-47 */
+      U[0] = U[1] = 0.;
+      U[2] = t <= 1. / 20 ? 2 * sin(20. * M_PI * t) : 0.;
+      return;
+    case PB_MAXWELL_WSCATTER: /* wscatter.cu:38-50 */
+      U[0] = U[1] = 0.;
+      U[2] = (y < .15 && y > -.15 && t < 0.5) ? sin(2. * M_PI * t) : 0.;
+      return;
+    default:
+      exact_state(o, U, x, y, t);
+  }
 }
 
 /* ghost state of a boundary side (eval_boundary, conserv_kernels.cu:820-843) */
@@ -317,8 +393,8 @@ static void ghost(const or_solver *o, int code, const double *UL, double *UR, do
     for (int n = 0; n < o->N; n++) UR[n] = UL[n];
     return;
   }
-  if (code == -3) { /* inflow: U_inflow = exact state */
-    exact_state(o, UR, x, y, t);
+  if (code == -3) { /* inflow: U_inflow */
+    inflow_state(o, UR, x, y, t);
     return;
   }
   if (code == -2) { /* outflow: Euler problems use the exact state; others leave zero */
@@ -355,8 +431,8 @@ static void ghost(const or_solver *o, int code, const double *UL, double *UR, do
   } else if (o->eq == EQ_MAXWELL) { /* maxwells/cmirror/cmirror.cu:63-77 */
     double dot = UL[0] * nx + UL[1] * ny;
     UR[2] = UL[2];
-    UR[0] = UL[0] - 2 * dot * nx;
-    UR[1] = UL[1] - 2 * dot * ny;
+    UR[0] = -UL[0] + 2 * dot * nx;
+    UR[1] = -UL[1] + 2 * dot * ny;
   }
 }
 
@@ -424,17 +500,23 @@ static double side_speed(const or_solver *o, const double *U, double nx, double 
   return s > 0. ? s + c : -s + c;
 }
 
+/* get_velocity (advection.cu:12) for an affine field */
+static void velocity(const or_solver *o, double x, double y, double *vx, double *vy) {
+  *vx = o->ax + o->agrad[0] * x + o->agrad[1] * y;
+  *vy = o->ay + o->agrad[2] * x + o->agrad[3] * y;
+}
+
+/* numerical flux at a point (x, y) of the side (advection needs it) */
 static void riemann(const or_solver *o, const double *UL, const double *UR, double nx, double ny,
-                    double *F) {
+                    double x, double y, double *F) {
   int N = o->N;
   if (o->eq == EQ_ADV) { /* upwind, advection.cu:94-116 */
-    double fxl[1], fyl[1], fxr[1], fyr[1];
-    flux(o, UL, fxl, fyl);
-    flux(o, UR, fxr, fyr);
-    if (nx * o->ax + ny * o->ay > 0)
-      F[0] = fxl[0] * nx + fyl[0] * ny;
+    double vx, vy;
+    velocity(o, x, y, &vx, &vy);
+    if (nx * vx + ny * vy > 0)
+      F[0] = vx * UL[0] * nx + vy * UL[0] * ny;
     else
-      F[0] = fxr[0] * nx + fyr[0] * ny;
+      F[0] = vx * UR[0] * nx + vy * UR[0] * ny;
     return;
   }
   double fxl[NMAX], fyl[NMAX], fxr[NMAX], fyr[NMAX], lam;
@@ -472,6 +554,13 @@ or_solver *or_create(int eq, int p, int K, int S, const double *V, const int *es
   o->eps = prm16[5];
   o->g = prm16[6];
   for (int i = 0; i < 8; i++) o->prm[i] = prm16[8 + i];
+  if (problem == PB_ADV_ROTATINGHILL || problem == PB_ADV_SPIN) {
+    /* the problem's rotation (-w y, w x) (rotatinghill.cu:37-40, spin.cu:37-40) */
+    double w = problem == PB_ADV_SPIN ? ROT_SPIN : ROT_HILL;
+    o->ax = o->ay = 0.;
+    o->agrad[1] = -w;
+    o->agrad[2] = w;
+  }
   exact_tables(o);
   o->V = (double *)xmalloc(sizeof(double) * 6 * K);
   memcpy(o->V, V, sizeof(double) * 6 * K);
@@ -542,6 +631,28 @@ or_solver *or_create(int eq, int p, int K, int S, const double *V, const int *es
 }
 
 /* shallow-water bed modes [mode][elem] (copied), or NULL for a flat bed */
+/* advection velocity field a = (ax, ay) + grad (x, y) */
+int or_set_field(or_solver *o, double ax, double ay, const double *grad) {
+  o->ax = ax;
+  o->ay = ay;
+  for (int i = 0; i < 4; i++) o->agrad[i] = grad ? grad[i] : 0.;
+  return 0;
+}
+
+/* inflow pressure series of the pulse problem */
+int or_set_series(or_solver *o, int n, const double *amp, const double *omega,
+                  const double *phase, double t0) {
+  if (n < 0 || n > NSER) return 1;
+  o->nser = n;
+  o->ser_t0 = t0;
+  for (int k = 0; k < n; k++) {
+    o->ser[k][0] = amp[k];
+    o->ser[k][1] = omega[k];
+    o->ser[k][2] = phase[k];
+  }
+  return 0;
+}
+
 int or_set_bathymetry(or_solver *o, const double *b) {
   free(o->bathy);
   o->bathy = 0;
@@ -649,17 +760,17 @@ static void dg_operator(or_solver *o, double *C, double t, double dt, double *ou
     memset(acc_r, 0, sizeof acc_r);
     for (int j = 0; j < n1; j++) {
       double UL[NMAX] = {0, 0, 0, 0}, UR[NMAX] = {0, 0, 0, 0}, F[NMAX];
+      double x = 0, y = 0;
       for (int i = 0; i < np; i++)
         for (int n = 0; n < N; n++) UL[n] += C[CI(n, i, L)] * o->E[lf][j][i];
+      if (R < 0 || o->eq == EQ_ADV) face_xy(o, L, lf, j, &x, &y);
       if (R < 0) {
-        double x, y;
-        face_xy(o, L, lf, j, &x, &y);
         ghost(o, R, UL, UR, x, y, t, nx, ny);
       } else {
         for (int i = 0; i < np; i++)
           for (int n = 0; n < N; n++) UR[n] += C[CI(n, i, R)] * o->E[rf][n1 - 1 - j][i];
       }
-      riemann(o, UL, UR, nx, ny, F);
+      riemann(o, UL, UR, nx, ny, x, y, F);
       for (int i = 0; i < np; i++)
         for (int n = 0; n < N; n++) {
           acc_l[n * NPM + i] += -len / 2 * (o->w1[j] * F[n] * o->E[lf][j][i]);
@@ -699,7 +810,15 @@ static void dg_operator(or_solver *o, double *C, double t, double dt, double *ou
         for (int i = 0; i < np; i++)
           for (int n = 0; n < N; n++) U[n] += C[CI(n, i, e)] * o->B[q][i];
       }
-      flux(o, U, fx, fy);
+      if (o->eq == EQ_ADV) { /* eval_flux with the velocity at the point */
+        double x, y, vx, vy;
+        vol_xy(o, e, q, &x, &y);
+        velocity(o, x, y, &vx, &vy);
+        fx[0] = vx * U[0];
+        fy[0] = vy * U[0];
+      } else {
+        flux(o, U, fx, fy);
+      }
       for (int i = 0; i < np; i++)
         for (int n = 0; n < N; n++)
           acc[n * NPM + i] += fx[n] * (o->GR[q][i] * ys - o->GS[q][i] * yr) +
@@ -803,8 +922,12 @@ static double elem_lambda(const or_solver *o, const double *C, int e, double t) 
   double U[NMAX];
   for (int n = 0; n < o->N; n++) U[n] = C[CI(n, 0, e)] * o->B[0][0];
   switch (o->eq) {
-    case EQ_ADV: /* advection.cu:157-183 (constant velocity) */
-      return sqrt(o->ax * o->ax + o->ay * o->ay);
+    case EQ_ADV: { /* advection.cu:157-183: the velocity at point n_q / 2 */
+      double x, y, vx, vy;
+      vol_xy(o, e, o->nq / 2, &x, &y);
+      velocity(o, x, y, &vx, &vy);
+      return sqrt(vx * vx + vy * vy);
+    }
     case EQ_EULER: { /* euler.cu:248-277 */
       double p = (o->gamma - 1.) * (U[3] - (U[1] * U[1] + U[2] * U[2]) / 2. / U[0]);
       double c = sqrt(o->gamma * p / U[0]);

@@ -61,6 +61,8 @@ def lib():
         L.or_set_threads.argtypes = [C.c_int]
         L.or_get_tables.argtypes = [C.c_void_p, _dp]
         L.or_set_bathymetry.argtypes = [C.c_void_p, _dp]
+        L.or_set_field.argtypes = [C.c_void_p, C.c_double, C.c_double, _dp]
+        L.or_set_series.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp, C.c_double]
         _L = L
     return _L
 
@@ -122,6 +124,20 @@ class Oracle:
         else:
             self._bathy = np.ascontiguousarray(b, dtype=np.float64).reshape(self.np, self.K)
             self.L.or_set_bathymetry(self.h, _d(self._bathy))
+
+    def set_field(self, ax, ay, grad=None):
+        """Advection velocity a = (ax, ay) + grad (x, y); grad = (dax/dx,
+        dax/dy, day/dx, day/dy) or None for a constant velocity."""
+        self._grad = None if grad is None else np.ascontiguousarray(grad, dtype=np.float64)
+        self.L.or_set_field(self.h, float(ax), float(ay),
+                            None if self._grad is None else _d(self._grad))
+
+    def set_series(self, amp, omega, phase, t0=0.0):
+        """Inflow pressure series of the pulse problem."""
+        self._ser = [np.ascontiguousarray(a, dtype=np.float64) for a in (amp, omega, phase)]
+        if self.L.or_set_series(self.h, len(self._ser[0]), *[_d(a) for a in self._ser],
+                                float(t0)):
+            raise ValueError("at most 16 series terms")
 
     def tables(self):
         """The oracle's tabulation in the reference's flat layout."""

@@ -42,15 +42,66 @@ enum {
   PB_EULER_SUPERSONIC = 5,
   PB_SW_HUMP = 6,
   PB_SW_TEST = 7,
-  PB_MAXWELL_PLANE = 8
+  PB_MAXWELL_PLANE = 8,
+  PB_EULER_AIRFOIL = 12,
+  PB_ADV_SQUAREHILL = 13,
+  PB_ADV_ROTATINGHILL = 14,
+  PB_ADV_SPIN = 15,
+  PB_MAXWELL_CMIRROR = 16,
+  PB_MAXWELL_WSCATTER = 17,
+  PB_EULER_PULSE = 18
 };
 static int g_problem = PB_NONE;
 static double g_prm[16];
 /* prm layout: 0 t, 1 gamma, 2 ax, 3 ay, 4 mu, 5 eps, 6 (unused), 7 cfl,
  * 8..15 problem parameters */
 
+/* rotatinghill.cu:58-67 (its U_inflow): the hill at the point rotated back */
+static double rotated_hill(double A, double x0, double y0, double r, double x, double y,
+                           double t) {
+  double c = cos(2 * M_PI * t), s = sin(2 * M_PI * t);
+  return A * exp(-(pow(x * c + y * s - x0, 2) + pow(-x * s + y * c - y0, 2)) / (2 * r * r));
+}
+
+/* tube.cu:52-97 with a short series in prm 8 t0, then (amp, omega, phase) x 2 */
+static void pulse_state(double *U, double t) {
+  double GAM = g_prm[1], p = 1.0;
+  t += g_prm[8];
+  for (int k = 0; k < 2; k++) p += g_prm[9 + 3 * k] * cos(g_prm[10 + 3 * k] * t + g_prm[11 + 3 * k]);
+  double rho = GAM * pow(p, (1. / GAM)), u = ((p - 1) / GAM), v = 0.0;
+  U[0] = rho;
+  U[1] = u * rho;
+  U[2] = v * rho;
+  U[3] = 0.5 * rho * (u * u + v * v) + (p / (GAM - 1.));
+}
+
 static void exact_state(double *U, double x, double y, double t) {
   switch (g_problem) {
+    case PB_EULER_AIRFOIL: {
+      /* airfoil.cu:22-27 (MACH .98, ALPHA 5) */
+      double GAM = g_prm[1], MACH = 0.98, ALPHA = 5.;
+      U[0] = GAM;
+      U[1] = U[0] * MACH * cos(M_PI * (ALPHA / 180.));
+      U[2] = U[0] * MACH * sin(M_PI * (ALPHA / 180.));
+      U[3] = 0.5 * U[0] * MACH * MACH + 1. / (GAM - 1.0);
+      break;
+    }
+    case PB_EULER_PULSE:
+      pulse_state(U, t);
+      break;
+    case PB_ADV_SQUAREHILL: {
+      /* squarehill.cu:22-30, translated by the velocity */
+      double xs = x - g_prm[2] * t, ys = y - g_prm[3] * t;
+      U[0] = (xs < -.2 && xs > -.8 && ys < .1 && ys > -.5) ? 1. : 0.;
+      break;
+    }
+    case PB_ADV_ROTATINGHILL:
+      U[0] = rotated_hill(5., 0.2, 0.0, 0.15, x, y, t);
+      break;
+    case PB_ADV_SPIN:
+      /* spin.cu:22-30 */
+      U[0] = exp(-((x - .5) * (x - .5) + (y - .5) * (y - .5)) / (2 * .1 * .1));
+      break;
     case PB_ADV_SINE: {
       /* u0 = sin(2 pi x) sin(2 pi y) translated by a t on the unit square */
       double xs = x - g_prm[2] * t, ys = y - g_prm[3] * t;
@@ -134,14 +185,42 @@ static void exact_state(double *U, double x, double y, double t) {
       break;
     }
     default:
-      for (int n = 0; n < 4; n++) U[n] = 0;
+      for (int n = 0; n < N; n++) U[n] = 0; /* the module's variable count */
   }
 }
 
 /* the problem plugin entry points the reference modules call */
-void U0(double *U, double x, double y) { exact_state(U, x, y, 0.0); }
+void U0(double *U, double x, double y) {
+  if (g_problem == PB_EULER_PULSE) { /* tube.cu:25-45: at rest */
+    double GAM = g_prm[1];
+    U[0] = GAM;
+    U[1] = U[2] = 0.;
+    U[3] = 1. / (GAM - 1.0);
+    return;
+  }
+  exact_state(U, x, y, 0.0);
+}
 void U_exact(double *U, double x, double y, double t) { exact_state(U, x, y, t); }
-void U_inflow(double *U, double x, double y, double t) { exact_state(U, x, y, t); }
+void U_inflow(double *U, double x, double y, double t) {
+  switch (g_problem) {
+    case PB_ADV_SQUAREHILL: /* squarehill.cu:43-45 */
+    case PB_ADV_SPIN:       /* spin.cu:43-46 */
+      U[0] = 0;
+      return;
+    case PB_MAXWELL_CMIRROR: /* cmirror.cu:38-47 */
+      U[0] = 0.;
+      U[1] = 0.;
+      U[2] = t <= 1. / 20 ? 2 * sin(M_PI * 20 * t) : 0.;
+      return;
+    case PB_MAXWELL_WSCATTER: /* wscatter.cu:38-50 (f = 1) */
+      U[0] = 0.;
+      U[1] = 0.;
+      U[2] = (y < .15 && y > -.15 && t < 1. / 2.) ? sin(M_PI * 2 * t) : 0.;
+      return;
+    default:
+      exact_state(U, x, y, t);
+  }
+}
 void U_outflow(double *U, double x, double y, double t) {
   /* exact.cu:50-52 and test.cu:53-55 leave the ghost state untouched;
    * supersonic.cu:55-57 uses U0; Euler problems here use the exact state */
@@ -149,9 +228,13 @@ void U_outflow(double *U, double x, double y, double t) {
     case PB_EULER_VORTEX:
     case PB_EULER_RIEMANN4:
     case PB_EULER_SUPERSONIC:
+    case PB_EULER_AIRFOIL: /* airfoil.cu:55-57: U0 */
+    case PB_EULER_PULSE:   /* tube.cu:107-109: U_inflow */
       exact_state(U, x, y, t);
       break;
     case PB_MAXWELL_PLANE:
+    case PB_MAXWELL_CMIRROR:  /* cmirror.cu:55-59 */
+    case PB_MAXWELL_WSCATTER: /* wscatter.cu:58-63 */
       U[0] = U[1] = U[2] = 0;
       break;
     default:
@@ -178,6 +261,18 @@ void U_reflection(double *U_left, double *U_right, double x, double y, double t,
       U_right[2] = -(U_left[1] * Ny - U_left[2] * Nx) * Nx;
       break;
     }
+    case PB_EULER_AIRFOIL: {
+      /* airfoil.cu:63-100: normal part reversed, tangential part kept */
+      double u_N, u_T;
+      U_right[0] = U_left[0];
+      U_right[3] = U_left[3];
+      u_N = -(nx * U_left[1] + ny * U_left[2]);
+      u_T = ny * U_left[1] - nx * U_left[2];
+      U_right[1] = u_N * nx + u_T * ny;
+      U_right[2] = u_N * ny - u_T * nx;
+      break;
+    }
+    case PB_EULER_PULSE: /* tube.cu:121-135: normal reflection */
     case PB_EULER_VORTEX:
     case PB_EULER_RIEMANN4: {
       /* slip wall: mirror the momentum about the face */
@@ -197,12 +292,15 @@ void U_reflection(double *U_left, double *U_right, double x, double y, double t,
       U_right[2] = U_left[2] - 2 * dot * ny;
       break;
     }
-    case PB_MAXWELL_PLANE: {
-      /* maxwells/cmirror/cmirror.cu:63-77: E_z kept, H mirrored */
+    case PB_MAXWELL_PLANE:
+    case PB_MAXWELL_CMIRROR:
+    case PB_MAXWELL_WSCATTER: {
+      /* maxwells/cmirror/cmirror.cu:63-77: E_z kept, normal H kept,
+       * tangential H reversed */
       double dot = U_left[0] * nx + U_left[1] * ny;
       U_right[2] = U_left[2];
-      U_right[0] = U_left[0] - 2 * dot * nx;
-      U_right[1] = U_left[1] - 2 * dot * ny;
+      U_right[0] = -U_left[0] + 2 * dot * nx;
+      U_right[1] = -U_left[1] + 2 * dot * ny;
       break;
     }
     default:
@@ -215,6 +313,18 @@ double get_GAMMA() { return g_prm[1]; }
 #endif
 #if defined(REF_ADVECTION) || defined(REF_SHALLOWWATER)
 void get_velocity(double *A, double x, double y, double t) {
+  if (g_problem == PB_ADV_ROTATINGHILL) { /* rotatinghill.cu:37-40 */
+    const double PI = 3.14159265358979323;
+    A[0] = -2 * PI * y;
+    A[1] = 2 * PI * x;
+    return;
+  }
+  if (g_problem == PB_ADV_SPIN) { /* spin.cu:37-40 */
+    const double PI = 3.14159;
+    A[0] = -2 * PI * y;
+    A[1] = 2 * PI * x;
+    return;
+  }
   A[0] = g_prm[2];
   A[1] = g_prm[3];
 }

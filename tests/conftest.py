@@ -39,6 +39,16 @@ def split_tables(tab, p):
     return out
 
 
+PB_PULSE = 18
+
+
+def pulse_series(d):
+    """(amp, omega, phase, t0) of a euler_pulse fixture: prm 8 holds t0 and
+    prm 9..14 two (amp, omega, phase) terms."""
+    prm = d["prm"]
+    return prm[[9, 12]], prm[[10, 13]], prm[[11, 14]], float(prm[8])
+
+
 def relerr(a, b, N):
     """max over variables of ||a_n - b_n|| / ||b_n|| (norm-wise, per variable block)."""
     a = np.asarray(a).reshape(N, -1)

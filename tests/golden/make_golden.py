@@ -139,6 +139,52 @@ def main():
         save("init_%s_p%d" % (name, p),
              run_ref(eq, p, 3, pb, mesh, np.zeros((N, dg.n_modes(p), mesh.K)), prm))
 
+    # problems whose boundary data are the point of the case: each RHS at a
+    # time where its inflow is active
+    pulse = (0.9197, 0.05, 4.47, 2.9, 0.03, 8.95, 2.66)  # t0, (amp, omega, phase) x 2
+    m_rot = dg.Mesh.square(6, 6, box=(-1, 1, -1, 1), jitter=0.1, seed=31, bc=(-3, -3, -3, -3))
+    m_spin = dg.Mesh.square(6, 6, jitter=0.1, seed=32, bc=(-3, -3, -3, -3))
+    m_sq = dg.Mesh.square(6, 6, box=(-1, 1, -1, 1), jitter=0.1, seed=33, bc=(-3, -2, -2, -2))
+    m_cm = dg.Mesh.square(6, 6, jitter=0.1, seed=34, bc=(-3, -2, -1, -1))
+    m_ws = dg.Mesh.square(6, 6, box=(-.5, .5, -.5, .5), jitter=0.1, seed=35, bc=(-3, -2, -1, -1))
+    m_af = dg.Mesh.square(5, 5, jitter=0.1, seed=36, bc=(-2, -2, -1, -1))
+    m_pu = dg.Mesh.square(8, 3, box=(0, 4, 0, 1), jitter=0.1, seed=37, bc=(-3, -2, -1, -1))
+    bcases = [
+        # name, eq, problem, mesh, prm (t in prm[0]), p list
+        ("adv_rotatinghill", dg.ADVECTION, PB["adv_rotatinghill"], m_rot,
+         prm_vec(t=0.1, ax=0, ay=0), [1, 2, 3]),
+        ("adv_spin", dg.ADVECTION, PB["adv_spin"], m_spin, prm_vec(t=0.1, ax=0, ay=0), [2]),
+        ("adv_squarehill", dg.ADVECTION, PB["adv_squarehill"], m_sq, prm_vec(t=0.1, ax=1, ay=0),
+         [1, 2]),
+        ("maxwell_cmirror", dg.MAXWELL, PB["maxwell_cmirror"], m_cm, prm_vec(t=0.02), [2]),
+        ("maxwell_wscatter", dg.MAXWELL, PB["maxwell_wscatter"], m_ws, prm_vec(t=0.2), [2]),
+        ("euler_airfoil", dg.EULER, PB["euler_airfoil"], m_af, prm_vec(t=0.1), [2]),
+        ("euler_pulse", dg.EULER, PB["euler_pulse"], m_pu, prm_vec(t=0.3, extra=pulse), [2]),
+    ]
+    for name, eq, pb, mesh, prm, plist in bcases:
+        for p in plist:
+            seed += 1
+            C = perturbed_ic(eq, p, pb, mesh, prm, seed)
+            save("rhs_%s_p%d" % (name, p), run_ref(eq, p, 0, pb, mesh, C, prm))
+        p = list(plist)[len(list(plist)) // 2]
+        N = dg.n_vars(eq)
+        save("init_%s_p%d" % (name, p),
+             run_ref(eq, p, 3, pb, mesh, np.zeros((N, dg.n_modes(p), mesh.K)), prm))
+    # wave speeds of the rotating fields (each element's speed at its middle
+    # quadrature point) and reference RK loops driven by them
+    for name, pb, mesh, p in [("adv_rotatinghill", PB["adv_rotatinghill"], m_rot, 2),
+                              ("adv_spin", PB["adv_spin"], m_spin, 1)]:
+        C = perturbed_ic(dg.ADVECTION, p, pb, mesh, prm_vec(ax=0, ay=0), 6)
+        save("cfl_%s_p%d" % (name, p), run_ref(dg.ADVECTION, p, 6, pb, mesh, C,
+                                               prm_vec(ax=0, ay=0)))
+    for name, pb, mesh, p, ns, rk, cfl in [
+            ("rk4_adv_rotatinghill_p2", PB["adv_rotatinghill"], m_rot, 2, 5, 4, 0.5),
+            ("rk2_adv_spin_p1", PB["adv_spin"], m_spin, 1, 5, 2, 0.7)]:
+        prm = prm_vec(ax=0, ay=0, cfl=cfl)
+        C = run_ref(dg.ADVECTION, p, 3, pb, mesh, np.zeros((1, dg.n_modes(p), mesh.K)), prm)["out"]
+        save(name, run_ref(dg.ADVECTION, p, 1, pb, mesh, C.reshape(1, -1, mesh.K), prm,
+                           nsteps=ns, rk=rk))
+
     # limiter (p = 1): discontinuous Euler data, noisy advection data
     m8 = dg.Mesh.square(8, 8, jitter=0.1, seed=21, bc=(-2, -2, -2, -2))
     C = perturbed_ic(dg.EULER, 1, PB["euler_riemann4"], m8, prm_vec(), 7, amp=0.05)

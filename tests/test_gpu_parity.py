@@ -6,7 +6,8 @@ right-hand side 1e-12, state after N steps 1e-10."""
 import numpy as np
 import pytest
 
-from conftest import golden_names, load_golden, ref_tables, relerr, split_tables
+from conftest import (PB_PULSE, golden_names, load_golden, pulse_series, ref_tables, relerr,
+                      split_tables)
 
 pytestmark = pytest.mark.gpu
 
@@ -31,6 +32,8 @@ def solver_for(dg, d, ref_tab=True, limiter=0):
     P = params_from(dg, d)
     P.limiter = limiter
     s = dg.Solver(mesh, int(d["eq"]), int(d["p"]), params=P)
+    if int(d["problem"]) == PB_PULSE:
+        s.set_inflow_series(*pulse_series(d))
     if ref_tab:
         s.set_tables(*split_tables(ref_tables(int(d["p"])), int(d["p"])))
     return s
@@ -50,6 +53,8 @@ def test_rhs_exact_basis_matches_oracle(dglib, oracle_mod, name):
     s = solver_for(dglib, d, ref_tab=False)
     o = oracle_mod.Oracle(int(d["eq"]), int(d["p"]), d["V"], d["es"], d["sxy"], d["se"], d["prm"],
                           int(d["problem"]))
+    if int(d["problem"]) == PB_PULSE:
+        o.set_series(*pulse_series(d))
     t = float(d["prm"][0])
     assert relerr(s.eval_rhs(d["C"].reshape(s.shape), t), o.rhs(d["C"], t), s.N) <= RHS_TOL
 

@@ -6,7 +6,7 @@ rounding error, bounded per order below."""
 import numpy as np
 import pytest
 
-from conftest import golden_names, load_golden, ref_tables, relerr
+from conftest import PB_PULSE, golden_names, load_golden, pulse_series, ref_tables, relerr
 
 CASES = [n for n in golden_names("") if not n.startswith("tables")]
 # reference basis-table error (relative, RHS): measured bound per order
@@ -16,6 +16,8 @@ EXACT_BOUND = {0: 1e-13, 1: 1e-12, 2: 1e-12, 3: 1e-11, 4: 2e-9, 5: 5e-7}
 def run_case(O, d, use_ref_tables):
     eq, p, mode, pb = int(d["eq"]), int(d["p"]), int(d["mode"]), int(d["problem"])
     o = O.Oracle(eq, p, d["V"], d["es"], d["sxy"], d["se"], d["prm"], pb)
+    if pb == PB_PULSE:
+        o.set_series(*pulse_series(d))
     if use_ref_tables:
         o.set_tables(ref_tables(p))
     t, out, N = float(d["prm"][0]), d["out"], o.N
