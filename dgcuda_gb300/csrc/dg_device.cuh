@@ -286,6 +286,7 @@ struct Advection {  // advection/advection.cu
   static constexpr bool kBathymetry = false;
   // the velocity may vary in space (q.field): fluxes then take the position
   static constexpr bool kField = true;
+  static constexpr bool kFolded = false;
   DG_HD static bool physical(const EqP &, const double *) { return true; }
   DG_HD static void flux(const EqP &q, const double *U, double *fx, double *fy) {
     fx[0] = q.ax * U[0];
@@ -355,22 +356,49 @@ struct Euler {  // euler/euler.cu
     fy[2] = fma(U[2], v, p);
     fy[3] = H * v;
   }
+  // the physical flux folded with the element metric, g = F . (ys, -xs) and
+  // h = F . (-yr, xr), the two integrands of the volume term (eval_volume,
+  // conserv_kernels.cu:1066-1074), formed from the momentum components
+  // along those directions without F_x and F_y: 26 FP64 operations where
+  // the flux and the fold take 33
+  static constexpr bool kFolded = true;
+  DG_HD static void flux_folded(const EqP &q, const double *U, double xr, double yr, double xs,
+                                double ys, double *g, double *h) {
+    const double ir = rcp(U[0]);
+    const double ma = fma(U[1], ys, -U[2] * xs), mb = fma(U[2], xr, -U[1] * yr);
+    const double ua = ma * ir, ub = mb * ir;
+    const double m2 = fma(U[1], U[1], U[2] * U[2]);
+    // p is reused as an addend: round it explicitly (never fused into an FMA)
+    const double p = mul_rn(q.gamma - 1., fma(-0.5 * m2, ir, U[3]));
+    const double H = U[3] + p;
+    g[0] = ma;
+    g[1] = fma(U[1], ua, p * ys);
+    g[2] = fma(U[2], ua, -p * xs);
+    g[3] = H * ua;
+    h[0] = mb;
+    h[1] = fma(U[1], ub, -p * yr);
+    h[2] = fma(U[2], ub, p * xr);
+    h[3] = H * ub;
+  }
   // local Lax-Friedrichs (euler.cu:170-237)
   static constexpr double kRawScale = 0.5;  // LLF: F = 0.5 [ ... ]
   DG_HD static void riemann_raw(const EqP &q, const double *UL, const double *UR, double nx,
                                 double ny, double *F) {
     // every multiply-add is an explicit fma so the rounding does not depend
-    // on how the compiler contracts the expression in a given kernel
-    double irl = rcp(UL[0]), irr = rcp(UR[0]);
-    double ul = UL[1] * irl, vl = UL[2] * irl, ur = UR[1] * irr, vr = UR[2] * irr;
-    double pl = mul_rn(q.gamma - 1., fma(-0.5, fma(UL[1], ul, UL[2] * vl), UL[3]));
-    double pr = mul_rn(q.gamma - 1., fma(-0.5, fma(UR[1], ur, UR[2] * vr), UR[3]));
-    double snl = fma(nx, ul, ny * vl), snr = fma(nx, ur, ny * vr);
-    double cl = sqrt(q.gamma * pl * irl), cr = sqrt(q.gamma * pr * irr);
-    double lam = fmax(fabs(snl) + cl, fabs(snr) + cr);
-    F[0] = fma(lam, UL[0] - UR[0], fma(UL[0], snl, UR[0] * snr));
-    F[1] = fma(lam, UL[1] - UR[1], fma(UL[1], snl, fma(pl, nx, fma(UR[1], snr, pr * nx))));
-    F[2] = fma(lam, UL[2] - UR[2], fma(UL[2], snl, fma(pl, ny, fma(UR[2], snr, pr * ny))));
+    // on how the compiler contracts the expression in a given kernel; the
+    // normal momenta m . n are the mass fluxes themselves
+    const double irl = rcp(UL[0]), irr = rcp(UR[0]);
+    const double mnl = fma(UL[1], nx, UL[2] * ny), mnr = fma(UR[1], nx, UR[2] * ny);
+    const double snl = mnl * irl, snr = mnr * irr;
+    const double m2l = fma(UL[1], UL[1], UL[2] * UL[2]), m2r = fma(UR[1], UR[1], UR[2] * UR[2]);
+    const double pl = mul_rn(q.gamma - 1., fma(-0.5 * m2l, irl, UL[3]));
+    const double pr = mul_rn(q.gamma - 1., fma(-0.5 * m2r, irr, UR[3]));
+    const double cl = sqrt(q.gamma * pl * irl), cr = sqrt(q.gamma * pr * irr);
+    const double lam = fmax(fabs(snl) + cl, fabs(snr) + cr);
+    const double P = pl + pr;
+    F[0] = fma(lam, UL[0] - UR[0], mnl + mnr);
+    F[1] = fma(lam, UL[1] - UR[1], fma(UL[1], snl, fma(UR[1], snr, P * nx)));
+    F[2] = fma(lam, UL[2] - UR[2], fma(UL[2], snl, fma(UR[2], snr, P * ny)));
     F[3] = fma(lam, UL[3] - UR[3], fma(UL[3] + pl, snl, (UR[3] + pr) * snr));
   }
   DG_HD static double mean_speed(const EqP &q, const double *U) {  // euler.cu:248-277
@@ -411,6 +439,7 @@ struct ShallowWater {  // shallowwater/shallowwater.cu (g is a parameter here)
   static constexpr int N = 3;
   static constexpr bool kBathymetry = true;  // optional bed b(x, y): source -g h grad b
   static constexpr bool kField = false;
+  static constexpr bool kFolded = false;
   DG_HD static bool physical(const EqP &, const double *U) { return U[0] >= 0.; }
   DG_HD static void flux(const EqP &q, const double *U, double *fx, double *fy) {
     double ih = rcp(U[0]);
@@ -453,6 +482,7 @@ struct Maxwell {  // maxwells/maxwells.cu, U = (Hx, Hy, Ez)
   static constexpr int N = 3;
   static constexpr bool kBathymetry = false;
   static constexpr bool kField = false;
+  static constexpr bool kFolded = false;
   DG_HD static bool physical(const EqP &, const double *) { return true; }
   DG_HD static void flux(const EqP &q, const double *U, double *fx, double *fy) {
     double imu = 1. / q.mu, ieps = 1. / q.eps;
@@ -483,6 +513,24 @@ struct Maxwell {  // maxwells/maxwells.cu, U = (Hx, Hy, Ez)
   }
   static constexpr bool outflow_uses_exact = false;
 };
+
+// the volume integrands g = F . (ys, -xs), h = F . (-yr, xr) of a state U
+// (eval_volume, conserv_kernels.cu:1066-1074): an equation's own folded
+// flux where it has one, else the flux and the fold
+template <class Eq>
+DG_HD void folded_flux(const EqP &q, const double *U, double xr, double yr, double xs, double ys,
+                       double *g, double *h) {
+  if constexpr (Eq::kFolded) {
+    Eq::flux_folded(q, U, xr, yr, xs, ys, g, h);
+  } else {
+    double fx[Eq::N], fy[Eq::N];
+    Eq::flux(q, U, fx, fy);
+    for (int n = 0; n < Eq::N; n++) {
+      g[n] = fma(fx[n], ys, -fy[n] * xs);
+      h[n] = fma(fy[n], xr, -fx[n] * yr);
+    }
+  }
+}
 
 // ghost state of a boundary side (eval_boundary, conserv_kernels.cu:820-843)
 template <class Eq>

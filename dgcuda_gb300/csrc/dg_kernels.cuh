@@ -199,7 +199,7 @@ __device__ __forceinline__ bool volume(const Tab<P> &tab, const EqP &q,
   bool ok = true;
 #pragma unroll
   for (int k = 0; k < NQ; k++) {
-    double U[N], fx[N], fy[N];
+    double U[N], gr[N], gs[N];
 #pragma unroll
     for (int n = 0; n < N; n++) {
       double a = c[n][0] * tab.B[k][0];
@@ -208,24 +208,27 @@ __device__ __forceinline__ bool volume(const Tab<P> &tab, const EqP &q,
       U[n] = a;
     }
     ok &= Eq::physical(q, U);
+    // [fx fy] [y_s -y_r; -x_s x_r] once per point (eval_volume :1066-1074)
     if constexpr (Eq::kField) {
       // velocity at the point x = x1 + xr r + xs s (get_coordinates_2d, :231-235)
-      double vx = q.ax, vy = q.ay;
+      double vx = q.ax, vy = q.ay, fx[N], fy[N];
       if (q.field)
         Eq::velocity(q, fma(xr, tab.r[k], fma(xs, tab.s[k], x1)),
                      fma(yr, tab.r[k], fma(ys, tab.s[k], y1)), vx, vy);
       Eq::flux_at(vx, vy, U, fx, fy);
+#pragma unroll
+      for (int n = 0; n < N; n++) {
+        gr[n] = fma(fx[n], ys, -fy[n] * xs);
+        gs[n] = fma(fy[n], xr, -fx[n] * yr);
+      }
     } else {
-      Eq::flux(q, U, fx, fy);
+      folded_flux<Eq>(q, U, xr, yr, xs, ys, gr, gs);
     }
-    // [fx fy] [y_s -y_r; -x_s x_r] folded once per point (eval_volume :1066-1074)
 #pragma unroll
     for (int n = 0; n < N; n++) {
-      const double gr = fma(fx[n], ys, -fy[n] * xs);
-      const double gs = fma(fy[n], xr, -fx[n] * yr);
 #pragma unroll
       for (int i = 1; i < NP; i++)  // grad phi_0 = 0
-        acc[n][i] = fma(tab.GR[k][i], gr, fma(tab.GS[k][i], gs, acc[n][i]));
+        acc[n][i] = fma(tab.GR[k][i], gr[n], fma(tab.GS[k][i], gs[n], acc[n][i]));
     }
     if (Eq::kBathymetry && bz) {
       // bed slope source S = (0, -g h b_x, -g h b_y) (the reference's
@@ -388,6 +391,29 @@ __global__ void __launch_bounds__(kMaxBlock) k_element(const __grid_constant__ T
 }
 
 // ---------------------------------------------------------------------------
+// Order-preserving integer view of a double: for non-NaN x, y,
+// x < y  <=>  order_key(x) < order_key(y) (with -0 just below +0).  Negative
+// values get their 63 low bits flipped, so signed 64-bit comparison follows
+// the real line.  The map is its own inverse.
+__device__ __forceinline__ long long order_key(double x) {
+  const long long b = __double_as_longlong(x);
+  return b ^ (long long)((unsigned long long)(b >> 63) >> 1);
+}
+__device__ __forceinline__ double from_order_key(long long k) {
+  return __longlong_as_double(k ^ (long long)((unsigned long long)(k >> 63) >> 1));
+}
+
+// bounds of the cell means over an element (c) and its three neighbours
+// (a, b, d), each mean the product c phi0: with phi0 > 0 the rounded product
+// is monotonic in c, so min_k (c_k phi0) = (min_k c_k) phi0 exactly, and the
+// extremes are found on the integer pipe
+__device__ __forceinline__ void mean_bounds(double c, double a, double b, double d, double phi0,
+                                            double &lo, double &hi) {
+  const long long kc = order_key(c), ka = order_key(a), kb = order_key(b), kd = order_key(d);
+  lo = __dmul_rn(from_order_key(min(min(kc, ka), min(kb, kd))), phi0);
+  hi = __dmul_rn(from_order_key(max(max(kc, ka), max(kb, kd))), phi0);
+}
+
 template <class Eq, int P>
 __global__ void __launch_bounds__(kMaxBlock) k_limit(const __grid_constant__ Tab<P> tab,
                                                   double *u, const int *__restrict__ nbr,
@@ -406,10 +432,8 @@ __global__ void __launch_bounds__(kMaxBlock) k_limit(const __grid_constant__ Tab
     // products reused as addends are rounded explicitly (__dmul_rn is never
     // fused into an FMA), so every kernel instance rounds them the same way
     const double Uc = __dmul_rn(c[0], phi0);
-    const double m0 = __dmul_rn(row[nb0], phi0), m1 = __dmul_rn(row[nb1], phi0),
-                 m2 = __dmul_rn(row[nb2], phi0);
-    const double Umin = fmin(Uc, fmin(m0, fmin(m1, m2)));
-    const double Umax = fmax(Uc, fmax(m0, fmax(m1, m2)));
+    double Umin, Umax;
+    mean_bounds(c[0], row[nb0], row[nb1], row[nb2], phi0, Umin, Umax);
     // largest overshoot above / below the mean over the edge points; the
     // reference takes min_j over (Uc-Umin)/(U_j-Uc) resp. (Uc-Umax)/(U_j-Uc)
     // (conserv_kernels.cu:694-705), which is the same number: division
@@ -443,18 +467,6 @@ __global__ void __launch_bounds__(kMaxBlock) k_limit(const __grid_constant__ Tab
   }
 }
 
-// Order-preserving integer view of a double: for non-NaN x, y,
-// x < y  <=>  order_key(x) < order_key(y) (with -0 just below +0).  Negative
-// values get their 63 low bits flipped, so signed 64-bit comparison follows
-// the real line.  The map is its own inverse.
-__device__ __forceinline__ long long order_key(double x) {
-  const long long b = __double_as_longlong(x);
-  return b ^ (long long)((unsigned long long)(b >> 63) >> 1);
-}
-__device__ __forceinline__ double from_order_key(long long k) {
-  return __longlong_as_double(k ^ (long long)((unsigned long long)(k >> 63) >> 1));
-}
-
 // ---------------------------------------------------------------------------
 // The same limiter reading the edge traces k_element<TR> left in T instead of
 // re-evaluating them; a limited variable's traces are rebuilt from its
@@ -478,10 +490,8 @@ __device__ __forceinline__ void limit_tr_body(const Tab<P> &tab, const EqP &q, d
     // products reused as addends are rounded explicitly (__dmul_rn is never
     // fused into an FMA), so every kernel instance rounds them the same way
     const double Uc = __dmul_rn(c0[n], phi0);
-    const double m0 = __dmul_rn(row[nb0], phi0), m1 = __dmul_rn(row[nb1], phi0),
-                 m2 = __dmul_rn(row[nb2], phi0);
-    const double Umin = fmin(Uc, fmin(m0, fmin(m1, m2)));
-    const double Umax = fmax(Uc, fmax(m0, fmax(m1, m2)));
+    double Umin, Umax;
+    mean_bounds(c0[n], row[nb0], row[nb1], row[nb2], phi0, Umin, Umax);
     // max_k (T_k - Uc) = max_k T_k - Uc exactly (rounding is monotonic), so
     // the extremes of the edge values are found first, on the integer pipe
     // (order_key), and each is subtracted once

@@ -416,17 +416,15 @@ __global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_const
     const double xs = geo[2 * (size_t)Kp + ec[e]], ys = geo[3 * (size_t)Kp + ec[e]];
 #pragma unroll
     for (int p = 0; p < PQ; p++) {
-      double u[N], fx[N], fy[N];
+      double u[N], gr[N], gs[N];
 #pragma unroll
       for (int n = 0; n < N; n++) u[n] = ub[((n * PQ + p) * 2 + e) * 32 + lane];
-      Eq::flux(q, u, fx, fy);
+      folded_flux<Eq>(q, u, xr, yr, xs, ys, gr, gs);
       const bool real = p * 4 + t < NQ;
 #pragma unroll
       for (int n = 0; n < N; n++) {
-        const double gr = fma(fx[n], ys, -fy[n] * xs);
-        const double gs = fma(fy[n], xr, -fx[n] * yr);
-        gh[(((p * 2 + e) * N + n) * 2 + 0) * 32 + lane] = real ? gr : 0.0;
-        gh[(((p * 2 + e) * N + n) * 2 + 1) * 32 + lane] = real ? gs : 0.0;
+        gh[(((p * 2 + e) * N + n) * 2 + 0) * 32 + lane] = real ? gr[n] : 0.0;
+        gh[(((p * 2 + e) * N + n) * 2 + 1) * 32 + lane] = real ? gs[n] : 0.0;
       }
     }
   }

@@ -681,7 +681,10 @@ extern "C" dg_status dg_solver_set_tables(dg_solver *s, int n_q, int n_1, const 
   }
   for (int v = 0; v < 3; v++)
     for (int i = 0; i < np; i++) t.V[v][i] = vertex[i * 3 + v];
-  // the kernels use that basis function 0 is constant (one edge value)
+  // the kernels use that basis function 0 is a positive constant (one edge
+  // value; the limiter's mean bounds need phi_0 > 0)
+  if (!(t.B[0][0] > 0))
+    return fail(DG_BAD_ARG, "basis function 0 must be positive");
   for (int f = 0; f < 3; f++)
     for (int j = 0; j < n_1; j++)
       if (t.E[f][j][0] != t.E[0][0][0])
