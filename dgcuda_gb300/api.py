@@ -110,6 +110,7 @@ def _declare(L):
         "dg_kernel_launches": (C.c_longlong, [C.c_void_p]),
         "dg_measure_fp64_peak": (C.c_int, [C.c_int, _dp]),
         "dg_probe_reciprocal": (C.c_int, [C.c_int, C.c_int, _dp, _dp, _dp]),
+        "dg_probe_physical": (C.c_int, [C.c_int, C.c_int, _dp, _ip, _ip]),
         "dg_eval_vertices": (C.c_int, [C.c_void_p, C.c_int, _dp]),
         "dg_eval_vertices_view": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, _dp]),
         "dg_save_checkpoint": (C.c_int, [C.c_void_p, C.c_char_p, C.c_double]),
@@ -224,6 +225,17 @@ class Adjoint:
 
     def __del__(self):
         self.close()
+
+
+def probe_physical(U, device=0):
+    """(fast, exact) decisions of the Euler positivity test for states U of
+    shape (n, 4) on the GPU: the single-precision filter and the FP64 test."""
+    L = load_library()
+    U = np.ascontiguousarray(U, dtype=np.float64).reshape(-1, 4)
+    n = U.shape[0]
+    fast, exact = np.zeros(n, dtype=np.int32), np.zeros(n, dtype=np.int32)
+    _check(L.dg_probe_physical(device, n, _dptr(U), _iptr(fast), _iptr(exact)))
+    return fast.astype(bool), exact.astype(bool)
 
 
 def params_for_problem(problem):

@@ -126,6 +126,34 @@ DG_HD double rcp(double x) {
 #endif
 }
 
+#ifdef __CUDACC__
+// x to single precision from its high word alone, with integer instructions:
+// sign, exponent rebiased, the top 20 of the 52 fraction bits (relative
+// error below 2^-20); NaN when x is outside the normal float range (or zero)
+__device__ __forceinline__ float f32_of_hi(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x);
+  const unsigned ex = (hi >> 20) & 0x7FFu;
+  const unsigned b = (hi & 0x80000000u) | ((ex - 896u) << 23) | ((hi & 0xFFFFFu) << 3);
+  return __uint_as_float(ex - 897u < 253u ? b : 0x7FC00000u);
+}
+
+// true only if the Euler state U (rho, m_x, m_y, E) is physical (rho >= 0,
+// 2 rho E >= |m|^2): with rho > 0 and a = 2 rho E in the normal range, a
+// and b = |m|^2 formed in single precision from 20-bit copies are each
+// within 2^-18.8 of the exact products, so a - b > 2^-16 (a + b) proves
+// 2 rho E > |m|^2 with room for the FP64 test's own rounding (2^-51).
+// False means "not settled here" (NaN, out of range, tiny, or close to the
+// boundary), never "non-physical"
+__device__ __forceinline__ bool physical_f32(const double *U) {
+  const float r = f32_of_hi(U[0]), mx = f32_of_hi(U[1]), my = f32_of_hi(U[2]),
+              E = f32_of_hi(U[3]);
+  const float a = __fmul_rn(__fmul_rn(2.0f, r), E);
+  const float b = __fmaf_rn(mx, mx, __fmul_rn(my, my));
+  return r > 0.0f && a > 1e-30f &&
+         __fsub_rn(a, b) > __fmul_rn(1.52587890625e-05f, __fadd_rn(a, b));
+}
+#endif
+
 // --------------------------------------------------------------------------
 // problem plugins: exact / initial / inflow state (U0, U_exact, U_inflow)
 // --------------------------------------------------------------------------
@@ -335,10 +363,19 @@ struct Euler {  // euler/euler.cu
   static constexpr bool kBathymetry = false;
   static constexpr bool kField = false;
   // rho >= 0 and p >= 0 (is_physical, euler.cu:76-86); with rho > 0,
-  // p < 0 <=> 2 rho E < |rho u|^2, which needs no FP64 division
-  DG_HD static bool physical(const EqP &, const double *U) {
+  // p < 0 <=> 2 rho E < |rho u|^2, which needs no FP64 division.  On the
+  // device a single-precision test settles almost every state first
+  // (physical_f32); only what it leaves open takes the FP64 test, so every
+  // decision is the FP64 test's
+  DG_HD static bool physical_fp64(const double *U) {
     if (U[0] < 0) return false;
     return !(2.0 * U[0] * U[3] < fma(U[1], U[1], U[2] * U[2]));
+  }
+  DG_HD static bool physical(const EqP &, const double *U) {
+#ifdef __CUDA_ARCH__
+    if (physical_f32(U)) return true;
+#endif
+    return physical_fp64(U);
   }
   DG_HD static void flux(const EqP &q, const double *U, double *fx, double *fy) {
     double ir = rcp(U[0]);

@@ -28,7 +28,44 @@ __global__ void k_reciprocal(const double *x, double *r, double *q, int n) {
     q[i] = 1.0 / x[i];
   }
 }
+__global__ void k_physical(const double *U, int *fast, int *exact, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const double *u = U + 4 * (size_t)i;
+    fast[i] = dg::physical_f32(u) ? 1 : 0;
+    exact[i] = dg::Euler::physical_fp64(u) ? 1 : 0;
+  }
+}
 }  // namespace
+
+// the Euler positivity test's single-precision filter and its FP64 test on
+// the device for n host states U[4 i .. 4 i + 3] = (rho, m_x, m_y, E):
+// fast[i] = 1 where the filter settles the state as physical, exact[i] = 1
+// where the FP64 test finds it physical
+extern "C" dg_status dg_probe_physical(int device, int n, const double *U, int *fast, int *exact) {
+  if (n < 0 || (n && (!U || !fast || !exact))) return dg::fail(DG_BAD_ARG, "bad arguments");
+  if (!n) return DG_OK;
+  if (cudaSetDevice(device) != cudaSuccess) return dg::fail(DG_CUDA_ERROR, "cudaSetDevice");
+  double *d = nullptr;
+  int *f = nullptr;
+  const size_t b = sizeof(double) * 4 * (size_t)n;
+  if (cudaMalloc(&d, b) != cudaSuccess) return dg::fail(DG_CUDA_ERROR, "cudaMalloc");
+  if (cudaMalloc(&f, 2 * sizeof(int) * (size_t)n) != cudaSuccess) {
+    cudaFree(d);
+    return dg::fail(DG_CUDA_ERROR, "cudaMalloc");
+  }
+  cudaError_t e = cudaMemcpy(d, U, b, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    k_physical<<<(n + 255) / 256, 256>>>(d, f, f + n, n);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(fast, f, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(exact, f + n, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  cudaFree(f);
+  return e == cudaSuccess ? DG_OK : dg::fail(DG_CUDA_ERROR, cudaGetErrorString(e));
+}
 
 // the flux kernels' reciprocal (dg::rcp) and IEEE division on the device for
 // n host values: r[i] = rcp(x[i]), q[i] = 1 / x[i]
