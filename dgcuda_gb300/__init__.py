@@ -12,4 +12,4 @@ from .api import (DGError, Mesh, Solver, Batch, Adjoint, Params, lib_path, load_
                   ADVECTION, EULER, SHALLOW_WATER, MAXWELL, SSP_RK3, RK4, RK2,
                   BC_REFLECT, BC_OUTFLOW, BC_INFLOW, BC_TRANSMISSIVE, PERIODIC, PROBLEMS,
                   n_modes, n_vars, measure_fp64_peak, probe_reciprocal, oz_table_image,
-                  params_for_problem, probe_physical)
+                  params_for_problem, probe_physical, probe_sqrt)

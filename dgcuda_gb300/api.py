@@ -111,6 +111,7 @@ def _declare(L):
         "dg_measure_fp64_peak": (C.c_int, [C.c_int, _dp]),
         "dg_probe_reciprocal": (C.c_int, [C.c_int, C.c_int, _dp, _dp, _dp]),
         "dg_probe_physical": (C.c_int, [C.c_int, C.c_int, _dp, _ip, _ip]),
+        "dg_probe_sqrt": (C.c_int, [C.c_int, C.c_int, _dp, _dp, _dp]),
         "dg_eval_vertices": (C.c_int, [C.c_void_p, C.c_int, _dp]),
         "dg_eval_vertices_view": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, _dp]),
         "dg_save_checkpoint": (C.c_int, [C.c_void_p, C.c_char_p, C.c_double]),
@@ -225,6 +226,15 @@ class Adjoint:
 
     def __del__(self):
         self.close()
+
+
+def probe_sqrt(x, device=0):
+    """(r, q): the sound speeds' square root and IEEE sqrt on the GPU."""
+    L = load_library()
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    r, q = np.empty_like(x), np.empty_like(x)
+    _check(L.dg_probe_sqrt(device, len(x), _dptr(x), _dptr(r), _dptr(q)))
+    return r, q
 
 
 def probe_physical(U, device=0):

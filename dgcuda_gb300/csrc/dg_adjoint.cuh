@@ -6,7 +6,8 @@
 //   V_i = sum_q GR_qi Gr_q + GS_qi Gs_q  + sum_q B_qi w_q J src_q
 //   S_i = -/+ sum_j (len/2) w_j F*(U_L(j), U_R(j); n) E_i(j)     (left / right)
 // Gr = fx ys - fy xs, Gs = fy xr - fx yr, src = (0, -g h b_x, -g h b_y).
-// Both derivative codes use the same hand-derived 3x3 Jacobians:
+// Both derivative codes use the same hand-derived 3x3 Jacobians, applied to
+// vectors without forming them (sw_jac_mul, sw_jac_tmul):
 //   A(U; n) = d(F(U).n)/dU, the physical normal flux of shallow water;
 //   Rusanov F* = 1/2 (F(U_L).n + F(U_R).n + lam (U_L - U_R)),
 //   lam = max(lam_L, lam_R), lam_X = |q_X / h_X| + sqrt(g h_X), q = m.n:
@@ -21,55 +22,54 @@
 
 namespace dg {
 
-// d(F(U).n)/dU for shallow water, U = (h, hu, hv)
-__device__ __forceinline__ void sw_flux_jac(double g, const double *U, double nx, double ny,
-                                            double A[3][3]) {
-  const double ih = 1.0 / U[0];
-  const double q = fma(U[1], nx, U[2] * ny);
-  const double qh = q * ih;
-  A[0][0] = 0.0;
-  A[0][1] = nx;
-  A[0][2] = ny;
-  A[1][0] = fma(-U[1] * ih, qh, g * U[0] * nx);
-  A[1][1] = fma(U[1] * ih, nx, qh);
-  A[1][2] = U[1] * ih * ny;
-  A[2][0] = fma(-U[2] * ih, qh, g * U[0] * ny);
-  A[2][1] = U[2] * ih * nx;
-  A[2][2] = fma(U[2] * ih, ny, qh);
+// A(U; n) = d(F(U).n)/dU for shallow water, U = (h, hu, hv), applied to a
+// vector without forming the matrix.  With u = hu/h, v = hv/h, qh = (hu,hv).n/h
+// and gh = g h the rows are
+//   [0, nx, ny],  [gh nx - u qh, u nx + qh, u ny],  [gh ny - v qh, v nx, v ny + qh].
+// y = A x
+__device__ __forceinline__ void sw_jac_mul(double u, double v, double qh, double gh, double nx,
+                                           double ny, const double *x, double *y) {
+  const double xn = fma(nx, x[1], ny * x[2]);
+  const double t = fma(-qh, x[0], xn);
+  const double g0 = gh * x[0];
+  y[0] = xn;
+  y[1] = fma(u, t, fma(qh, x[1], g0 * nx));
+  y[2] = fma(v, t, fma(qh, x[2], g0 * ny));
+}
+// z = A^T f
+__device__ __forceinline__ void sw_jac_tmul(double u, double v, double qh, double gh, double nx,
+                                            double ny, const double *f, double *z) {
+  const double wf = fma(u, f[1], v * f[2]);
+  const double fn = fma(nx, f[1], ny * f[2]);
+  const double fw = f[0] + wf;
+  z[0] = fma(-qh, wf, gh * fn);
+  z[1] = fma(nx, fw, qh * f[1]);
+  z[2] = fma(ny, fw, qh * f[2]);
 }
 
-// lam_X and its gradient
-__device__ __forceinline__ double sw_lambda(double g, const double *U, double nx, double ny,
-                                            double dl[3]) {
-  const double ih = 1.0 / U[0];
-  const double s = fma(U[1], nx, U[2] * ny) * ih;
-  const double c = sqrt(U[0] * g);
-  const double sg = s >= 0.0 ? 1.0 : -1.0;
-  dl[0] = fma(sg, -s * ih, 0.5 * g / c);
-  dl[1] = sg * nx * ih;
-  dl[2] = sg * ny * ih;
-  return fabs(s) + c;
+// one trace of a side: the pieces of A(U; n), c = sqrt(g h) and
+// lam = |qh| + c
+struct SwTrace {
+  double ih, u, v, qh, gh, c, lam;
+};
+__device__ __forceinline__ SwTrace sw_trace(double g, const double *U, double nx, double ny) {
+  SwTrace w;
+  w.ih = rcp(U[0]);
+  w.u = U[1] * w.ih;
+  w.v = U[2] * w.ih;
+  w.qh = fma(U[1], nx, U[2] * ny) * w.ih;
+  w.gh = g * U[0];
+  w.c = sqrt_pos(w.gh);
+  w.lam = fabs(w.qh) + w.c;
+  return w;
 }
-
-// Jacobians of the Rusanov flux with respect to the two traces
-__device__ __forceinline__ void sw_rusanov_jac(double g, const double *UL, const double *UR,
-                                               double nx, double ny, double AL[3][3],
-                                               double AR[3][3]) {
-  double dlL[3], dlR[3];
-  const double lL = sw_lambda(g, UL, nx, ny, dlL), lR = sw_lambda(g, UR, nx, ny, dlR);
-  const bool left = lL >= lR;
-  const double lam = left ? lL : lR;
-  sw_flux_jac(g, UL, nx, ny, AL);
-  sw_flux_jac(g, UR, nx, ny, AR);
-#pragma unroll
-  for (int a = 0; a < 3; a++) {
-    const double d = UL[a] - UR[a];
-#pragma unroll
-    for (int b = 0; b < 3; b++) {
-      AL[a][b] = 0.5 * (AL[a][b] + (a == b ? lam : 0.0) + (left ? d * dlL[b] : 0.0));
-      AR[a][b] = 0.5 * (AR[a][b] - (a == b ? lam : 0.0) + (left ? 0.0 : d * dlR[b]));
-    }
-  }
+// d lam / dU = (-sg qh / h + c / (2 h), sg nx / h, sg ny / h), sg = sign(qh)
+// (d sqrt(g h)/dh = g / (2 c) = c / (2 h))
+__device__ __forceinline__ void sw_dlam(const SwTrace &w, double nx, double ny, double dl[3]) {
+  const double sih = w.qh >= 0.0 ? w.ih : -w.ih;
+  dl[0] = fma(-w.qh, sih, 0.5 * w.c * w.ih);
+  dl[1] = sih * nx;
+  dl[2] = sih * ny;
 }
 
 // d(ghost)/d(U_L) of a boundary code (reflect mirrors the momentum,
@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(kBlock)
   const double *VR = inner ? Tv + ((size_t)sd.y * 3 + sd.w) * (N1 * N) : nullptr;
 #pragma unroll
   for (int j = 0; j < N1; j++) {
-    double UL[N], UR[N], AL[3][3], AR[3][3], M[3][3];
+    double UL[N], UR[N], M[3][3];
 #pragma unroll
     for (int n = 0; n < N; n++) UL[n] = TL[j * N + n];
     if (inner) {
@@ -153,10 +153,17 @@ __global__ void __launch_bounds__(kBlock)
       ghost_state<ShallowWater>(q, sd.y, UL, UR, 0.0, 0.0, 0.0, nx, ny);
       sw_ghost_jac(sd.y, nx, ny, M);
     }
-    sw_rusanov_jac(q.g, UL, UR, nx, ny, AL, AR);
-    const double sc = hl * tab.w1[j];
+    // Rusanov: dF*/dU_L = 1/2 (A_L + lam I + d dlam_L^T), dF*/dU_R = 1/2 (A_R
+    // - lam I + d dlam_R^T), d = U_L - U_R, the dlam term on the side of the
+    // max only; the 1/2 goes into the edge scale
+    const SwTrace wL = sw_trace(q.g, UL, nx, ny), wR = sw_trace(q.g, UR, nx, ny);
+    const bool left = wL.lam >= wR.lam;
+    const double lam = left ? wL.lam : wR.lam;
+    double dl[3];
+    sw_dlam(left ? wL : wR, nx, ny, dl);
+    const double sc = 0.5 * hl * tab.w1[j];
     if (!ADJ) {
-      double dUL[N], dUR[N];
+      double dUL[N], dUR[N], aL[N], aR[N];
 #pragma unroll
       for (int n = 0; n < N; n++) dUL[n] = VL[j * N + n];
       if (inner) {
@@ -167,11 +174,13 @@ __global__ void __launch_bounds__(kBlock)
         for (int a = 0; a < N; a++)
           dUR[a] = fma(M[a][0], dUL[0], fma(M[a][1], dUL[1], M[a][2] * dUL[2]));
       }
+      sw_jac_mul(wL.u, wL.v, wL.qh, wL.gh, nx, ny, dUL, aL);
+      sw_jac_mul(wR.u, wR.v, wR.qh, wR.gh, nx, ny, dUR, aR);
+      const double *dX = left ? dUL : dUR;
+      const double dlam = fma(dl[0], dX[0], fma(dl[1], dX[1], dl[2] * dX[2]));
 #pragma unroll
       for (int a = 0; a < N; a++) {
-        double v = 0.0;
-#pragma unroll
-        for (int b = 0; b < N; b++) v = fma(AL[a][b], dUL[b], fma(AR[a][b], dUR[b], v));
+        const double v = fma(UL[a] - UR[a], dlam, fma(lam, dUL[a] - dUR[a], aL[a] + aR[a]));
         out0[(size_t)s * (N1 * N) + j * N + a] = v * sc;
       }
     } else {
@@ -182,16 +191,15 @@ __global__ void __launch_bounds__(kBlock)
         Fb[n] = sc * (r - VL[j * N + n]);
       }
       double bL[N], bR[N];
+      sw_jac_tmul(wL.u, wL.v, wL.qh, wL.gh, nx, ny, Fb, bL);
+      sw_jac_tmul(wR.u, wR.v, wR.qh, wR.gh, nx, ny, Fb, bR);
+      const double dF = fma(UL[0] - UR[0], Fb[0], fma(UL[1] - UR[1], Fb[1], (UL[2] - UR[2]) * Fb[2]));
 #pragma unroll
       for (int b = 0; b < N; b++) {
-        double l = 0.0, r = 0.0;
-#pragma unroll
-        for (int a = 0; a < N; a++) {
-          l = fma(AL[a][b], Fb[a], l);
-          r = fma(AR[a][b], Fb[a], r);
-        }
-        bL[b] = l;
-        bR[b] = r;
+        bL[b] = fma(lam, Fb[b], bL[b]);
+        bR[b] = fma(-lam, Fb[b], bR[b]);
+        if (left) bL[b] = fma(dl[b], dF, bL[b]);
+        else bR[b] = fma(dl[b], dF, bR[b]);
       }
       if (!inner) {  // U_R = ghost(U_L): its adjoint returns to U_L
 #pragma unroll
@@ -253,7 +261,7 @@ __global__ void __launch_bounds__(kBlock)
   }
 #pragma unroll
   for (int k = 0; k < NQ; k++) {
-    double U[N], Ax[3][3], Ay[3][3];
+    double U[N];
 #pragma unroll
     for (int n = 0; n < N; n++) {
       double a = c[n][0] * tab.B[k][0];
@@ -261,8 +269,9 @@ __global__ void __launch_bounds__(kBlock)
       for (int i = 1; i < NP; i++) a = fma(c[n][i], tab.B[k][i], a);
       U[n] = a;
     }
-    sw_flux_jac(g, U, 1.0, 0.0, Ax);
-    sw_flux_jac(g, U, 0.0, 1.0, Ay);
+    // A_x = A(U; (1, 0)) and A_y = A(U; (0, 1)): qh is u resp. v
+    const double ih = rcp(U[0]);
+    const double uu = U[1] * ih, vv = U[2] * ih, gh = g * U[0];
     double br = 0.0, bs = 0.0;
 #pragma unroll
     for (int i = 1; i < NP; i++) {
@@ -279,15 +288,12 @@ __global__ void __launch_bounds__(kBlock)
         for (int i = 1; i < NP; i++) a = fma(v[n][i], tab.B[k][i], a);
         dU[n] = a;
       }
+      double dfx[N], dfy[N];
+      sw_jac_mul(uu, vv, uu, gh, 1.0, 0.0, dU, dfx);
+      sw_jac_mul(uu, vv, vv, gh, 0.0, 1.0, dU, dfy);
 #pragma unroll
       for (int n = 0; n < N; n++) {
-        double dfx = 0.0, dfy = 0.0;
-#pragma unroll
-        for (int m = 0; m < N; m++) {
-          dfx = fma(Ax[n][m], dU[m], dfx);
-          dfy = fma(Ay[n][m], dU[m], dfy);
-        }
-        const double gr = fma(dfx, ys, -dfy * xs), gs = fma(dfy, xr, -dfx * yr);
+        const double gr = fma(dfx[n], ys, -dfy[n] * xs), gs = fma(dfy[n], xr, -dfx[n] * yr);
 #pragma unroll
         for (int i = 1; i < NP; i++)
           acc[n][i] = fma(tab.GR[k][i], gr, fma(tab.GS[k][i], gs, acc[n][i]));
@@ -320,17 +326,16 @@ __global__ void __launch_bounds__(kBlock)
         Gr[n] = a;
         Gs[n] = b;
       }
+      double fxb[N], fyb[N], zx[N], zy[N];
 #pragma unroll
-      for (int m = 0; m < N; m++) {
-        double ub = 0.0;
-#pragma unroll
-        for (int n = 0; n < N; n++) {
-          const double fxb = fma(ys, Gr[n], -yr * Gs[n]);
-          const double fyb = fma(xr, Gs[n], -xs * Gr[n]);
-          ub = fma(Ax[n][m], fxb, fma(Ay[n][m], fyb, ub));
-        }
-        Ub[m] = ub;
+      for (int n = 0; n < N; n++) {
+        fxb[n] = fma(ys, Gr[n], -yr * Gs[n]);
+        fyb[n] = fma(xr, Gs[n], -xs * Gr[n]);
       }
+      sw_jac_tmul(uu, vv, uu, gh, 1.0, 0.0, fxb, zx);
+      sw_jac_tmul(uu, vv, vv, gh, 0.0, 1.0, fyb, zy);
+#pragma unroll
+      for (int m = 0; m < N; m++) Ub[m] = zx[m] + zy[m];
       if (bbar) {
         double Sx = 0.0, Sy = 0.0;
 #pragma unroll

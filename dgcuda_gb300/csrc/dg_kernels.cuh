@@ -325,13 +325,14 @@ __device__ __forceinline__ void element_body(const Tab<P> &tab, const EqP &q, co
     const int sd = a.esd[(size_t)f * Kp + e];
     const bool right = sd & 1;
     const double *F = a.Fh + (size_t)(sd >> 1) * (N1 * N);
-    const double sg = right ? 1.0 : -1.0;
+    // the sign as a bit flip (exactly -F), off the FP64 pipe
+    const long long sg = right ? 0ll : (long long)0x8000000000000000ull;
 #pragma unroll
     for (int j = 0; j < N1; j++) {
       const int jj = right ? (N1 - 1 - j) : j;
 #pragma unroll
       for (int n = 0; n < N; n++) {
-        const double fv = sg * F[jj * N + n];
+        const double fv = __longlong_as_double(sg ^ __double_as_longlong(F[jj * N + n]));
 #pragma unroll
         for (int i = 0; i < NP; i++) acc[n][i] = fma(fv, tab.E[f][j][i], acc[n][i]);
       }

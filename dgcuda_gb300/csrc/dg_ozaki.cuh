@@ -379,7 +379,7 @@ __global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_const
 
   // ---- side-flux offsets and signs of the element's edge points ----
   int foff[PF][2];
-  double fsg[PF][2];
+  long long fsg[PF][2];  // sign bit of the side flux on this face (-F left, +F right)
 #pragma unroll
   for (int p = 0; p < PF; p++)
 #pragma unroll
@@ -390,10 +390,10 @@ __global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_const
         const int sd = a.esd[(size_t)f * Kp + ec[e]];
         const bool right = sd & 1;
         foff[p][e] = (sd >> 1) * (N1 * N) + (right ? (N1 - 1 - j) : j) * N;
-        fsg[p][e] = right ? 1.0 : -1.0;
+        fsg[p][e] = right ? 0ll : (long long)0x8000000000000000ull;
       } else {
         foff[p][e] = 0;
-        fsg[p][e] = 0.0;
+        fsg[p][e] = 0ll;
       }
     }
 #pragma unroll
@@ -454,7 +454,8 @@ __global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_const
           xg[e][p] = p < PQ ? gh[(((p * 2 + e) * N + n) * 2 + 0) * 32 + lane] : 0.0;
           xh[e][p] = p < PQ ? gh[(((p * 2 + e) * N + n) * 2 + 1) * 32 + lane] : 0.0;
           xf[e][p] = (p < PF && p * 4 + t < NF)
-                         ? fsg[p < PF ? p : 0][e] * a.Fh[foff[p < PF ? p : 0][e] + n]
+                         ? __longlong_as_double(fsg[p < PF ? p : 0][e] ^
+                                                __double_as_longlong(a.Fh[foff[p < PF ? p : 0][e] + n]))
                          : 0.0;
         }
       constexpr bool kMerge = 2 * NQ + NF <= 36;

@@ -28,6 +28,13 @@ __global__ void k_reciprocal(const double *x, double *r, double *q, int n) {
     q[i] = 1.0 / x[i];
   }
 }
+__global__ void k_sqrt(const double *x, double *r, double *q, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    r[i] = dg::sqrt_pos(x[i]);
+    q[i] = __dsqrt_rn(x[i]);
+  }
+}
 __global__ void k_physical(const double *U, int *fast, int *exact, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) {
@@ -64,6 +71,26 @@ extern "C" dg_status dg_probe_physical(int device, int n, const double *U, int *
     e = cudaMemcpy(exact, f + n, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost);
   cudaFree(d);
   cudaFree(f);
+  return e == cudaSuccess ? DG_OK : dg::fail(DG_CUDA_ERROR, cudaGetErrorString(e));
+}
+
+// the sound speed's square root (dg::sqrt_pos) and IEEE sqrt on the device
+// for n host values: r[i] = sqrt_pos(x[i]), q[i] = sqrt(x[i])
+extern "C" dg_status dg_probe_sqrt(int device, int n, const double *x, double *r, double *q) {
+  if (n < 0 || (n && (!x || !r || !q))) return dg::fail(DG_BAD_ARG, "bad arguments");
+  if (!n) return DG_OK;
+  if (cudaSetDevice(device) != cudaSuccess) return dg::fail(DG_CUDA_ERROR, "cudaSetDevice");
+  double *d = nullptr;
+  const size_t b = sizeof(double) * (size_t)n;
+  if (cudaMalloc(&d, 3 * b) != cudaSuccess) return dg::fail(DG_CUDA_ERROR, "cudaMalloc");
+  cudaError_t e = cudaMemcpy(d, x, b, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    k_sqrt<<<(n + 255) / 256, 256>>>(d, d + n, d + 2 * (size_t)n, n);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(r, d + n, b, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(q, d + 2 * (size_t)n, b, cudaMemcpyDeviceToHost);
+  cudaFree(d);
   return e == cudaSuccess ? DG_OK : dg::fail(DG_CUDA_ERROR, cudaGetErrorString(e));
 }
 

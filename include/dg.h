@@ -340,6 +340,9 @@ dg_status dg_measure_fp64_peak(int device, double *tflops);
  * approximate reciprocal) and IEEE division, on the device, for n host
  * values: r[i] = rcp(x[i]), q[i] = 1 / x[i] (a check of the former) */
 dg_status dg_probe_reciprocal(int device, int n, const double *x, double *r, double *q);
+/* the sound speed's square root and IEEE sqrt on the device: r[i] =
+ * sqrt_pos(x[i]), q[i] = sqrt(x[i]) (checks) */
+dg_status dg_probe_sqrt(int device, int n, const double *x, double *r, double *q);
 /* the Euler positivity test (rho >= 0, p >= 0) on the device for n states
  * U[4i..4i+3] = (rho, m_x, m_y, E): fast[i] = 1 where its single-precision
  * filter settles the state as physical, exact[i] = 1 where the FP64 test

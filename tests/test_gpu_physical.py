@@ -50,3 +50,22 @@ def test_filter_settles_ordinary_states(dglib):
     assert exact.all() and fast.all()
     fast, exact = dg.probe_physical(states(rho, u, v, -p))
     assert not exact.any() and not fast.any()
+
+
+def test_sound_speed_sqrt_within_one_ulp(dglib):
+    """The face kernel's square root against IEEE sqrt on the GPU, over the
+    whole positive normal range and the special values (which take IEEE
+    sqrt)."""
+    dg = dglib
+    rng = np.random.default_rng(13)
+    x = 10.0 ** rng.uniform(-300, 300, 300000)
+    x = np.concatenate([x, rng.uniform(0.5, 2.0, 100000), 2.0 ** np.arange(-1022, 1024, 1.0),
+                        np.nextafter(2.0 ** np.arange(-1021, 1023, 1.0), 0),
+                        [0.0, -0.0, 5e-324, 1e-310, np.inf, np.nan, -1.0, 1.4, 2.0, 4.0]])
+    r, q = dg.probe_sqrt(x)
+    ok = np.isfinite(q) & (q > 0)
+    ulp = np.abs(r[ok] - q[ok]) / np.spacing(q[ok])
+    assert ulp.max() <= 1.0
+    assert np.array_equal(r[~ok], q[~ok], equal_nan=True)
+    with np.errstate(invalid="ignore"):
+        assert np.array_equal(q, np.sqrt(x), equal_nan=True)
