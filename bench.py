@@ -357,7 +357,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--p", type=int, default=3)
     ap.add_argument("--n", type=int, default=1024, help="squares per side")
-    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-sweep", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--ensemble", type=int, default=256,
@@ -453,6 +453,11 @@ def main():
     if args.e2e_steps > 0:
         host = torch.empty((N, npm, K), dtype=torch.float64, pin_memory=True)
         h = host.numpy()
+        s.get_state(out=h)
+        # one untimed round trip: the first single step after the profiled
+        # region captures and instantiates its CUDA graph
+        s.set_state(h)
+        t = s.step(1, dg.SSP_RK3, t)
         s.get_state(out=h)
         torch.cuda.synchronize()
         t0 = time.perf_counter()

@@ -51,6 +51,10 @@ struct dg_solver {
   bool has_inout_bc = false;      // a side with an inflow or outflow code
   void *oz = nullptr;             // tensor-core tables (Euler, p = 1..4)
   int *flag = nullptr;            // device flag of put_state
+  // host transfers of the state: a copy stream and one event per chunk of
+  // rows, so that the permutation of one chunk overlaps the copy of the next
+  cudaStream_t cst = nullptr;
+  std::vector<cudaEvent_t> cev;
   bool tensor = true;             // use them in the fused element stage
   // T holds the traces of U as the last fused SSP-RK3 stage left them (and U
   // is already limited): the next dg_step continues without recomputing
@@ -631,6 +635,9 @@ extern "C" void dg_solver_destroy(dg_solver *s) {
     cudaEventDestroy(pe.b);
   }
   for (auto e : s->pool) cudaEventDestroy(e);
+  if (s->cst) cudaStreamSynchronize(s->cst);
+  for (auto e : s->cev) cudaEventDestroy(e);
+  if (s->cst) cudaStreamDestroy(s->cst);
   for (void *p : s->allocs) cudaFree(p);
   if (s->st) cudaStreamDestroy(s->st);
   delete s;
@@ -709,23 +716,35 @@ extern "C" dg_status dg_init(dg_solver *s) {
   return sync_check(s);
 }
 
-// writes the state; when the stored traces were current and the new state
-// is bitwise the old one (a state read out and handed back unchanged), they
-// stay current, so the next dg_step continues exactly as if the state had
-// never left the device
-static dg_status put_state(dg_solver *s, const double *user) {
-  const bool keep = s->tr_valid;
+// rows [r0, r0 + nr) of the state from the caller's layout into U; with
+// `flag`, sets *flag when a value changes
+static void put_rows(dg_solver *s, const double *user, int r0, int nr, int *flag) {
+  const double *src = user + (size_t)r0 * s->K;
+  double *dst = s->U + (size_t)r0 * s->m.Kp;
+  if (flag) dg::launch_permute_in_cmp(s->st, src, dst, s->m.perm, nr, s->K, s->m.Kp, flag);
+  else dg::launch_permute_in(s->st, src, dst, s->m.perm, nr, s->K, s->m.Kp);
+}
+
+// before a put: when the stored traces were current, a flag (cleared here)
+// that records whether the state changes
+static dg_status begin_put(dg_solver *s, bool &keep) {
+  keep = s->tr_valid;
   s->tr_valid = false;
-  if (!keep) {
-    dg::launch_permute_in(s->st, user, s->U, s->m.perm, s->N * s->np, s->K, s->m.Kp);
-    return sync_check(s);
-  }
+  if (!keep) return DG_OK;
   if (!s->flag) {
     dg_status st = dalloc(s, &s->flag, 1);
     if (st != DG_OK) return st;
   }
   CK(cudaMemsetAsync(s->flag, 0, sizeof(int), s->st));
-  dg::launch_permute_in_cmp(s->st, user, s->U, s->m.perm, s->N * s->np, s->K, s->m.Kp, s->flag);
+  return DG_OK;
+}
+
+// after a put: when the stored traces were current and the new state is
+// bitwise the old one (a state read out and handed back unchanged), they
+// stay current, so the next dg_step continues exactly as if the state had
+// never left the device
+static dg_status end_put(dg_solver *s, bool keep) {
+  if (!keep) return sync_check(s);
   int changed = 1;
   CK(cudaMemcpyAsync(&changed, s->flag, sizeof(int), cudaMemcpyDeviceToHost, s->st));
   dg_status st = sync_check(s);
@@ -733,20 +752,81 @@ static dg_status put_state(dg_solver *s, const double *user) {
   return st;
 }
 
+static dg_status put_state(dg_solver *s, const double *user) {
+  bool keep;
+  dg_status st = begin_put(s, keep);
+  if (st != DG_OK) return st;
+  put_rows(s, user, 0, s->N * s->np, keep ? s->flag : nullptr);
+  return end_put(s, keep);
+}
+
+// rows per chunk of a host transfer (the whole state below 16 MB) and the
+// copy stream with its events
+static int transfer_chunks(dg_solver *s, int &per) {
+  const int rows = s->N * s->np;
+  const size_t bytes = (size_t)rows * s->K * sizeof(double);
+  per = bytes < ((size_t)16 << 20) ? rows : (rows + 7) / 8;
+  const int n = (rows + per - 1) / per;
+  if (!s->cst && cudaStreamCreateWithFlags(&s->cst, cudaStreamNonBlocking) != cudaSuccess) {
+    s->cst = nullptr;
+    return 0;
+  }
+  while ((int)s->cev.size() < n + 1) {
+    cudaEvent_t e;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return 0;
+    s->cev.push_back(e);
+  }
+  return n;
+}
+
+// host -> device in chunks of rows on the copy stream, each chunk permuted
+// on the solver stream as soon as it has arrived
 extern "C" dg_status dg_set_state(dg_solver *s, const double *C) {
   if (!s || !C) return fail(DG_BAD_ARG, "null argument");
   CK(cudaSetDevice(s->device));
-  size_t n = (size_t)s->N * s->np * s->K;
-  CK(cudaMemcpyAsync(s->ubuf, C, n * sizeof(double), cudaMemcpyHostToDevice, s->st));
-  return put_state(s, s->ubuf);
+  int per = 0;
+  const int nch = transfer_chunks(s, per);
+  if (!nch) return fail(DG_CUDA_ERROR, "copy stream or events");
+  bool keep;
+  dg_status st = begin_put(s, keep);
+  if (st != DG_OK) return st;
+  const int rows = s->N * s->np;
+  const size_t K = s->K;
+  // ubuf may still be read by earlier work on the solver stream
+  CK(cudaEventRecord(s->cev[nch], s->st));
+  CK(cudaStreamWaitEvent(s->cst, s->cev[nch], 0));
+  for (int c = 0; c < nch; c++) {
+    const int r0 = c * per, nr = std::min(per, rows - r0);
+    CK(cudaMemcpyAsync(s->ubuf + r0 * K, C + r0 * K, nr * K * sizeof(double),
+                       cudaMemcpyHostToDevice, s->cst));
+    CK(cudaEventRecord(s->cev[c], s->cst));
+    CK(cudaStreamWaitEvent(s->st, s->cev[c], 0));
+    put_rows(s, s->ubuf, r0, nr, keep ? s->flag : nullptr);
+  }
+  return end_put(s, keep);
 }
 
+// device -> host: each chunk of rows permuted on the solver stream, then
+// copied on the copy stream while the next chunk is permuted
 extern "C" dg_status dg_get_state(dg_solver *s, double *C) {
   if (!s || !C) return fail(DG_BAD_ARG, "null argument");
   CK(cudaSetDevice(s->device));
-  size_t n = (size_t)s->N * s->np * s->K;
-  dg::launch_permute_out(s->st, s->U, s->ubuf, s->m.perm, s->N * s->np, s->K, s->m.Kp);
-  CK(cudaMemcpyAsync(C, s->ubuf, n * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+  int per = 0;
+  const int nch = transfer_chunks(s, per);
+  if (!nch) return fail(DG_CUDA_ERROR, "copy stream or events");
+  const int rows = s->N * s->np;
+  const size_t K = s->K, Kp = s->m.Kp;
+  for (int c = 0; c < nch; c++) {
+    const int r0 = c * per, nr = std::min(per, rows - r0);
+    dg::launch_permute_out(s->st, s->U + r0 * Kp, s->ubuf + r0 * K, s->m.perm, nr, s->K, s->m.Kp);
+    CK(cudaEventRecord(s->cev[c], s->st));
+    CK(cudaStreamWaitEvent(s->cst, s->cev[c], 0));
+    CK(cudaMemcpyAsync(C + r0 * K, s->ubuf + r0 * K, nr * K * sizeof(double),
+                       cudaMemcpyDeviceToHost, s->cst));
+  }
+  // the solver stream waits for the copies (later work may overwrite ubuf)
+  CK(cudaEventRecord(s->cev[nch], s->cst));
+  CK(cudaStreamWaitEvent(s->st, s->cev[nch], 0));
   return sync_check(s);
 }
 
