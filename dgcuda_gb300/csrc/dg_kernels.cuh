@@ -455,8 +455,10 @@ __global__ void __launch_bounds__(kMaxBlock) k_limit(const __grid_constant__ Tab
     // a >= b > 0 (IEEE division is monotonic): divide only when it limits
     double alpha = 1.0;
     const double lo = Uc - Umin, hi = Umax - Uc;
-    if (up > lo) alpha = fmin(alpha, lo / up);
-    if (dn > hi) alpha = fmin(alpha, hi / dn);
+    // lo, hi >= +0; where a bound has collapsed (a uniform neighbourhood:
+    // lo or hi is +0, tested on its bits) the quotient is +0 without dividing
+    if (up > lo) alpha = fmin(alpha, __double_as_longlong(lo) ? lo / up : 0.0);
+    if (dn > hi) alpha = fmin(alpha, __double_as_longlong(hi) ? hi / dn : 0.0);
     if (alpha < 0.0) alpha = 0.0;
     if (alpha < 1.0) {
       double *w = u + (size_t)(n * NP) * Kp;
@@ -509,8 +511,10 @@ __device__ __forceinline__ void limit_tr_body(const Tab<P> &tab, const EqP &q, d
     // a >= b > 0 (IEEE division is monotonic): divide only when it limits
     double alpha = 1.0;
     const double lo = Uc - Umin, hi = Umax - Uc;
-    if (up > lo) alpha = fmin(alpha, lo / up);
-    if (dn > hi) alpha = fmin(alpha, hi / dn);
+    // lo, hi >= +0; where a bound has collapsed (a uniform neighbourhood:
+    // lo or hi is +0, tested on its bits) the quotient is +0 without dividing
+    if (up > lo) alpha = fmin(alpha, __double_as_longlong(lo) ? lo / up : 0.0);
+    if (dn > hi) alpha = fmin(alpha, __double_as_longlong(hi) ? hi / dn : 0.0);
     if (alpha < 0.0) alpha = 0.0;
     if (alpha < 1.0) {
       const double c1 = row[(size_t)1 * Kp + e] * alpha, c2 = row[(size_t)2 * Kp + e] * alpha;
