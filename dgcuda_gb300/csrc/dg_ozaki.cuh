@@ -260,10 +260,22 @@ template <class Eq, int P>
 struct OzShape {
   static constexpr int N = Eq::N, NP = Tab<P>::NP, NQ = Tab<P>::NQ, N1 = Tab<P>::N1, NF = 3 * N1;
   static constexpr int PM = npos(NP), PQ = npos(NQ), PF = npos(NF);
-  static constexpr int GH = 2 * PQ * 2 * N;                    // g, h per (point, element, var)
-  static constexpr int UB = N * (PQ > PF ? PQ : PF) * 2;       // area values, then traces
-  static constexpr size_t kSmem = (size_t)4 * (GH + UB) * 32 * sizeof(double);
+  // g, h per (position, row, variable) and lane; the area values and the
+  // new traces live in the same slots (gh_slot)
+  static constexpr int GH = 2 * PQ * 2 * N;
+  static_assert(PF <= 2 * PQ, "the traces of a variable fit its g, h slots");
+  static constexpr size_t kSmem = (size_t)4 * GH * 32 * sizeof(double);
 };
+
+// per-warp staging, one column per lane: slot k (0: g, 1: h) of variable n
+// at position p of row e.  An area value u(n, p, e) sits in the g slot of
+// its own (p, e), which the flux phase reads before writing g and h there;
+// the new trace at position p' of variable n goes to slot (p' / 2, e,
+// p' % 2) of that variable, whose g and h the projection has already read
+template <int N>
+__device__ __forceinline__ int gh_slot(int n, int p, int e, int k) {
+  return (((p * 2 + e) * N + n) * 2 + k) * 32;
+}
 
 template <class Eq, int P>
 constexpr size_t oz_smem_bytes() { return OzShape<Eq, P>::kSmem; }
@@ -294,8 +306,7 @@ __global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_const
   static_assert(NP <= 16 && NQ <= 16 && NF <= 16, "p <= 4");
   extern __shared__ __align__(16) double smem_d[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, t = lane & 3;
-  double *gh = smem_d + (size_t)warp * (S::GH + S::UB) * 32;
-  double *ub = gh + S::GH * 32;
+  double *gh = smem_d + (size_t)warp * S::GH * 32;
   const int K = a.K, Kp = a.Kp;
   const int e0 = (blockIdx.x * 4 + warp) * 16 + (lane >> 2);
   const int el[2] = {e0, e0 + 8};
@@ -342,7 +353,7 @@ __global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_const
     for (int p = 0; p < PQ; p++)
 #pragma unroll
       for (int e = 0; e < 2; e++)
-        ub[((n * PQ + p) * 2 + e) * 32 + lane] =
+        gh[gh_slot<N>(n, p, e, 0) + lane] =
             recombine(acc, p >> 1, 2 * e + (p & 1), m[e], ozt->colexp[kEval][slot_of(p, t)]);
   }
 
@@ -355,7 +366,7 @@ __global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_const
       if (p * 4 + t >= NQ) continue;
       double u[N];
 #pragma unroll
-      for (int n = 0; n < N; n++) u[n] = ub[((n * PQ + p) * 2 + e) * 32 + lane];
+      for (int n = 0; n < N; n++) u[n] = gh[gh_slot<N>(n, p, e, 0) + lane];
       badv[e] |= !Eq::physical(q, u);
     }
 #pragma unroll
@@ -371,7 +382,7 @@ __global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_const
 #pragma unroll
         for (int p = 0; p < PQ; p++) {
           const int idx = p * 4 + t;
-          ub[((n * PQ + p) * 2 + e) * 32 + lane] = c0 * tab.B[idx < NQ ? idx : 0][0];
+          gh[gh_slot<N>(n, p, e, 0) + lane] = c0 * tab.B[idx < NQ ? idx : 0][0];
         }
       }
     }
@@ -418,13 +429,13 @@ __global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_const
     for (int p = 0; p < PQ; p++) {
       double u[N], gr[N], gs[N];
 #pragma unroll
-      for (int n = 0; n < N; n++) u[n] = ub[((n * PQ + p) * 2 + e) * 32 + lane];
+      for (int n = 0; n < N; n++) u[n] = gh[gh_slot<N>(n, p, e, 0) + lane];
       folded_flux<Eq>(q, u, xr, yr, xs, ys, gr, gs);
       const bool real = p * 4 + t < NQ;
 #pragma unroll
       for (int n = 0; n < N; n++) {
-        gh[(((p * 2 + e) * N + n) * 2 + 0) * 32 + lane] = real ? gr[n] : 0.0;
-        gh[(((p * 2 + e) * N + n) * 2 + 1) * 32 + lane] = real ? gs[n] : 0.0;
+        gh[gh_slot<N>(n, p, e, 0) + lane] = real ? gr[n] : 0.0;
+        gh[gh_slot<N>(n, p, e, 1) + lane] = real ? gs[n] : 0.0;
       }
     }
   }
@@ -451,8 +462,8 @@ __global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_const
       for (int e = 0; e < 2; e++)
 #pragma unroll
         for (int p = 0; p < 4; p++) {
-          xg[e][p] = p < PQ ? gh[(((p * 2 + e) * N + n) * 2 + 0) * 32 + lane] : 0.0;
-          xh[e][p] = p < PQ ? gh[(((p * 2 + e) * N + n) * 2 + 1) * 32 + lane] : 0.0;
+          xg[e][p] = p < PQ ? gh[gh_slot<N>(n, p < PQ ? p : 0, e, 0) + lane] : 0.0;
+          xh[e][p] = p < PQ ? gh[gh_slot<N>(n, p < PQ ? p : 0, e, 1) + lane] : 0.0;
           xf[e][p] = (p < PF && p * 4 + t < NF)
                          ? __longlong_as_double(fsg[p < PF ? p : 0][e] ^
                                                 __double_as_longlong(a.Fh[foff[p < PF ? p : 0][e] + n]))
@@ -535,7 +546,7 @@ __global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_const
     for (int p = 0; p < PF; p++)
 #pragma unroll
       for (int e = 0; e < 2; e++)
-        ub[((n * PF + p) * 2 + e) * 32 + lane] =
+        gh[gh_slot<N>(n, p >> 1, e, p & 1) + lane] =
             recombine(acc, p >> 1, 2 * e + (p & 1), m[e], ozt->colexp[kTrace][slot_of(p, t)]);
   }
 
@@ -550,7 +561,7 @@ __global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_const
       if (p * 4 + t >= NF) continue;
       double u[N];
 #pragma unroll
-      for (int n = 0; n < N; n++) u[n] = ub[((n * PF + p) * 2 + e) * 32 + lane];
+      for (int n = 0; n < N; n++) u[n] = gh[gh_slot<N>(n, p >> 1, e, p & 1) + lane];
       badt[e] |= !Eq::physical(q, u);
     }
 #pragma unroll
@@ -576,7 +587,8 @@ __global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_const
       const int f = idx / N1, j = idx % N1;
 #pragma unroll
       for (int n = 0; n < N; n++)
-        Te[idx * N + n] = badt[e] ? c0[n] * tab.E[f][j][0] : ub[((n * PF + p) * 2 + e) * 32 + lane];
+        Te[idx * N + n] =
+            badt[e] ? c0[n] * tab.E[f][j][0] : gh[gh_slot<N>(n, p >> 1, e, p & 1) + lane];
     }
   }
   if (badt[0] || badt[1]) {
