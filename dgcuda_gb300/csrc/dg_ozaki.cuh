@@ -294,8 +294,11 @@ __device__ __forceinline__ void split_rows(const double (&x)[2][4], int (&m)[2],
   }
 }
 
+// 4 blocks per SM where registers allow it without heavy spills (p <= 2;
+// at p = 3 the spills at 128 registers cost more than the extra warps
+// bring, at p = 4 the shared memory holds 3 blocks)
 template <class Eq, int P>
-__global__ void __launch_bounds__(kOzThreads, 3) k_element_oz(const __grid_constant__ Tab<P> tab,
+__global__ void __launch_bounds__(kOzThreads, P <= 2 ? 4 : 3) k_element_oz(const __grid_constant__ Tab<P> tab,
                                                            const __grid_constant__ EqP q,
                                                            const __grid_constant__ ElemArgs a,
                                                            const Tabs *__restrict__ ozt) {
