@@ -182,11 +182,9 @@ __device__ __forceinline__ void contract(Acc &acc, const long long (&Y)[2][4], c
 // instructions only: S as a 128-bit two's complement pair, its magnitude
 // normalised by a leading-zero count, 53 bits kept, the rest as round and
 // sticky bits.
-__device__ __forceinline__ double recombine(const Acc &acc, int cg, int r, int m, int M) {
-  if (m == 0) return 0.0;  // an all-zero (or denormal-only) row
-  int d[kWeights];
-#pragma unroll
-  for (int w = 0; w < kWeights; w++) d[w] = __float_as_int(acc.d[w][cg][r]) - kAccBits;
+static __device__ __noinline__ double recombine_sums(int d0, int d1, int d2, int d3, int d4, int d5,
+                                             int d6, int d7, int m, int M) {
+  const int d[kWeights] = {d0, d1, d2, d3, d4, d5, d6, d7};
   const long long Sh = (long long)d[0] * 65536 + (long long)d[1] * 256 + d[2];  // |Sh| < 2^39
   const long long Sl = (long long)d[3] * 4294967296ll + (long long)d[4] * 16777216 +
                        (long long)d[5] * 65536 + (long long)d[6] * 256 + d[7];  // |Sl| < 2^55
@@ -229,6 +227,17 @@ __device__ __forceinline__ double recombine(const Acc &acc, int cg, int r, int m
   // out of the normal range: scale in two steps (never on physical data)
   const double v = ldexp((double)(long long)mant, ex);
   return ldexp(neg ? -v : v, k);
+}
+
+// one copy of the recombination for every call site (the kernel's hot loop
+// then fits the instruction cache); the class sums leave the accumulator in
+// registers
+__device__ __forceinline__ double recombine(const Acc &acc, int cg, int r, int m, int M) {
+  if (m == 0) return 0.0;  // an all-zero (or denormal-only) row
+  int d[kWeights];
+#pragma unroll
+  for (int w = 0; w < kWeights; w++) d[w] = __float_as_int(acc.d[w][cg][r]) - kAccBits;
+  return recombine_sums(d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7], m, M);
 }
 
 // a hint that the line holding p will be read soon (no register is held)
@@ -294,11 +303,10 @@ __device__ __forceinline__ void split_rows(const double (&x)[2][4], int (&m)[2],
   }
 }
 
-// 4 blocks per SM where registers allow it without heavy spills (p <= 2;
-// at p = 3 the spills at 128 registers cost more than the extra warps
-// bring, at p = 4 the shared memory holds 3 blocks)
+// 4 blocks per SM (128 registers) up to p = 3, where the extra warps hide
+// more latency than the spills cost; at p = 4 the shared memory holds 3
 template <class Eq, int P>
-__global__ void __launch_bounds__(kOzThreads, P <= 2 ? 4 : 3) k_element_oz(const __grid_constant__ Tab<P> tab,
+__global__ void __launch_bounds__(kOzThreads, P <= 3 ? 4 : 3) k_element_oz(const __grid_constant__ Tab<P> tab,
                                                            const __grid_constant__ EqP q,
                                                            const __grid_constant__ ElemArgs a,
                                                            const Tabs *__restrict__ ozt) {
