@@ -468,64 +468,125 @@ __global__ void __launch_bounds__(kOzThreads, P <= 3 ? 4 : 3) k_element_oz(const
     {  // volume (K blocks GR, GS over the area points) and surface (K block E
        // over the edge points) into one accumulator when the exactness
        // bound allows it (7 * 36 * 2^14 < 2^22), else two
-      double xg[2][4], xh[2][4], xf[2][4];
-#pragma unroll
-      for (int e = 0; e < 2; e++)
-#pragma unroll
-        for (int p = 0; p < 4; p++) {
-          xg[e][p] = p < PQ ? gh[gh_slot<N>(n, p < PQ ? p : 0, e, 0) + lane] : 0.0;
-          xh[e][p] = p < PQ ? gh[gh_slot<N>(n, p < PQ ? p : 0, e, 1) + lane] : 0.0;
-          xf[e][p] = (p < PF && p * 4 + t < NF)
-                         ? __longlong_as_double(fsg[p < PF ? p : 0][e] ^
-                                                __double_as_longlong(a.Fh[foff[p < PF ? p : 0][e] + n]))
-                         : 0.0;
-        }
-      constexpr bool kMerge = 2 * NQ + NF <= 36;
-      int m[2], mf[2];
-#pragma unroll
-      for (int e = 0; e < 2; e++) {
-        int mv = 0, ms = 0;
-#pragma unroll
-        for (int p = 0; p < 4; p++) {
-          mv = max(mv, max(bexp(xg[e][p]), bexp(xh[e][p])));
-          ms = max(ms, bexp(xf[e][p]));
-        }
-        if (kMerge) mv = max(mv, ms);
-        m[e] = quad_max(mv);
-        mf[e] = kMerge ? m[e] : quad_max(ms);
-      }
-      long long Y[2][4];
-      acc.reset();
-#pragma unroll
-      for (int e = 0; e < 2; e++)
-#pragma unroll
-        for (int p = 0; p < 4; p++) Y[e][p] = to_fixed(xg[e][p], max(m[e], 1));
-      contract<3, (PM + 1) / 2, (PQ <= 2)>(acc, Y, W + word_off(kProj), 0, lane);
-#pragma unroll
-      for (int e = 0; e < 2; e++)
-#pragma unroll
-        for (int p = 0; p < 4; p++) Y[e][p] = to_fixed(xh[e][p], max(m[e], 1));
-      contract<3, (PM + 1) / 2, (PQ <= 2)>(acc, Y, W + word_off(kProj), 1, lane);
-      if (!kMerge) {
-#pragma unroll
-        for (int p = 0; p < PM; p++)
-#pragma unroll
-          for (int e = 0; e < 2; e++)
-            R[p][e] = recombine(acc, p >> 1, 2 * e + (p & 1), m[e], ozt->colexp[kProj][slot_of(p, t)]);
-        acc.reset();
-      }
-#pragma unroll
-      for (int e = 0; e < 2; e++)
-#pragma unroll
-        for (int p = 0; p < 4; p++) Y[e][p] = to_fixed(xf[e][p], max(mf[e], 1));
-      contract<3, (PM + 1) / 2, (PF <= 2)>(acc, Y, W + word_off(kProj), 2, lane);
-#pragma unroll
-      for (int p = 0; p < PM; p++)
-#pragma unroll
+      // p = 3: one copy of the slicing and MMAs for the
+      // three K blocks, rolled; elsewhere three unrolled copies measure faster
+      if constexpr (P == 3) {
+        // K block kb's input at position p of row e: g, h (kb = 0, 1) from the
+        // staging slots, the side fluxes (kb = 2: -F on a left face, +F on a
+        // right face) from L1
+        auto xin = [&](int kb, int e, int p) -> double {
+          if (kb < 2) return p < PQ ? gh[gh_slot<N>(n, p < PQ ? p : 0, e, kb) + lane] : 0.0;
+          return (p < PF && p * 4 + t < NF)
+                     ? __longlong_as_double(fsg[p < PF ? p : 0][e] ^
+                                            __double_as_longlong(a.Fh[foff[p < PF ? p : 0][e] + n]))
+                     : 0.0;
+        };
+        constexpr bool kMerge = 2 * NQ + NF <= 36;
+        int m[2], mf[2];
+  #pragma unroll
         for (int e = 0; e < 2; e++) {
-          const double v = recombine(acc, p >> 1, 2 * e + (p & 1), mf[e], ozt->colexp[kProj][slot_of(p, t)]);
-          R[p][e] = kMerge ? v : R[p][e] + v;
+          int mv = 0, ms = 0;
+  #pragma unroll
+          for (int p = 0; p < 4; p++) {
+            mv = max(mv, max(bexp(xin(0, e, p)), bexp(xin(1, e, p))));
+            ms = max(ms, bexp(xin(2, e, p)));
+          }
+          if (kMerge) mv = max(mv, ms);
+          m[e] = quad_max(mv);
+          mf[e] = kMerge ? m[e] : quad_max(ms);
         }
+        long long Y[2][4];
+        acc.reset();
+        // one copy of the slicing and the MMAs for the three K blocks where
+        // they share the MMA shape (keeps the loop body in the instruction
+        // cache)
+        constexpr bool kSameShape = (PQ <= 2) == (PF <= 2);
+  #pragma unroll 1
+        for (int kb = 0; kb < 3; kb++) {
+          if (kb == 2 && !kMerge) {
+  #pragma unroll
+            for (int p = 0; p < PM; p++)
+  #pragma unroll
+              for (int e = 0; e < 2; e++)
+                R[p][e] = recombine(acc, p >> 1, 2 * e + (p & 1), m[e], ozt->colexp[kProj][slot_of(p, t)]);
+            acc.reset();
+          }
+  #pragma unroll
+          for (int e = 0; e < 2; e++)
+  #pragma unroll
+            for (int p = 0; p < 4; p++) Y[e][p] = to_fixed(xin(kb, e, p), max(kb == 2 ? mf[e] : m[e], 1));
+          if (kSameShape || kb < 2)
+            contract<3, (PM + 1) / 2, (PQ <= 2)>(acc, Y, W + word_off(kProj), kb, lane);
+          else
+            contract<3, (PM + 1) / 2, (PF <= 2)>(acc, Y, W + word_off(kProj), kb, lane);
+        }
+  #pragma unroll
+        for (int p = 0; p < PM; p++)
+  #pragma unroll
+          for (int e = 0; e < 2; e++) {
+            const double v = recombine(acc, p >> 1, 2 * e + (p & 1), mf[e], ozt->colexp[kProj][slot_of(p, t)]);
+            R[p][e] = kMerge ? v : R[p][e] + v;
+          }
+      } else {
+        double xg[2][4], xh[2][4], xf[2][4];
+  #pragma unroll
+        for (int e = 0; e < 2; e++)
+  #pragma unroll
+          for (int p = 0; p < 4; p++) {
+            xg[e][p] = p < PQ ? gh[gh_slot<N>(n, p < PQ ? p : 0, e, 0) + lane] : 0.0;
+            xh[e][p] = p < PQ ? gh[gh_slot<N>(n, p < PQ ? p : 0, e, 1) + lane] : 0.0;
+            xf[e][p] = (p < PF && p * 4 + t < NF)
+                           ? __longlong_as_double(fsg[p < PF ? p : 0][e] ^
+                                                  __double_as_longlong(a.Fh[foff[p < PF ? p : 0][e] + n]))
+                           : 0.0;
+          }
+        constexpr bool kMerge = 2 * NQ + NF <= 36;
+        int m[2], mf[2];
+  #pragma unroll
+        for (int e = 0; e < 2; e++) {
+          int mv = 0, ms = 0;
+  #pragma unroll
+          for (int p = 0; p < 4; p++) {
+            mv = max(mv, max(bexp(xg[e][p]), bexp(xh[e][p])));
+            ms = max(ms, bexp(xf[e][p]));
+          }
+          if (kMerge) mv = max(mv, ms);
+          m[e] = quad_max(mv);
+          mf[e] = kMerge ? m[e] : quad_max(ms);
+        }
+        long long Y[2][4];
+        acc.reset();
+  #pragma unroll
+        for (int e = 0; e < 2; e++)
+  #pragma unroll
+          for (int p = 0; p < 4; p++) Y[e][p] = to_fixed(xg[e][p], max(m[e], 1));
+        contract<3, (PM + 1) / 2, (PQ <= 2)>(acc, Y, W + word_off(kProj), 0, lane);
+  #pragma unroll
+        for (int e = 0; e < 2; e++)
+  #pragma unroll
+          for (int p = 0; p < 4; p++) Y[e][p] = to_fixed(xh[e][p], max(m[e], 1));
+        contract<3, (PM + 1) / 2, (PQ <= 2)>(acc, Y, W + word_off(kProj), 1, lane);
+        if (!kMerge) {
+  #pragma unroll
+          for (int p = 0; p < PM; p++)
+  #pragma unroll
+            for (int e = 0; e < 2; e++)
+              R[p][e] = recombine(acc, p >> 1, 2 * e + (p & 1), m[e], ozt->colexp[kProj][slot_of(p, t)]);
+          acc.reset();
+        }
+  #pragma unroll
+        for (int e = 0; e < 2; e++)
+  #pragma unroll
+          for (int p = 0; p < 4; p++) Y[e][p] = to_fixed(xf[e][p], max(mf[e], 1));
+        contract<3, (PM + 1) / 2, (PF <= 2)>(acc, Y, W + word_off(kProj), 2, lane);
+  #pragma unroll
+        for (int p = 0; p < PM; p++)
+  #pragma unroll
+          for (int e = 0; e < 2; e++) {
+            const double v = recombine(acc, p >> 1, 2 * e + (p & 1), mf[e], ozt->colexp[kProj][slot_of(p, t)]);
+            R[p][e] = kMerge ? v : R[p][e] + v;
+          }
+      }
     }
     // RK combination (element_body's epilogue)
     double cnew[2][4];
