@@ -1079,15 +1079,16 @@ const dg::BatchOps *batch_ops_for(dg_equation eq) {
   return nullptr;
 }
 
-// block -> problem maps for blocks of `blk` elements (or sides)
-void block_maps(const std::vector<int> &count, int blk, std::vector<int> &b2p,
-                std::vector<int> &b0) {
+// block -> problem maps for blocks of `blk` elements (or sides), the
+// problems visited in `order` (each problem's blocks stay contiguous)
+void block_maps(const std::vector<int> &count, const std::vector<int> &order, int blk,
+                std::vector<int> &b2p, std::vector<int> &b0) {
   b2p.clear();
   b0.assign(count.size(), 0);
-  for (size_t i = 0; i < count.size(); i++) {
+  for (int i : order) {
     b0[i] = (int)b2p.size();
     int nb = (count[i] + blk - 1) / blk;
-    for (int k = 0; k < nb; k++) b2p.push_back((int)i);
+    for (int k = 0; k < nb; k++) b2p.push_back(i);
   }
 }
 
@@ -1097,10 +1098,19 @@ dg_status batch_build_maps(dg_batch *b) {
     ke.push_back(s->K);
     ks.push_back(s->S);
   }
+  // problems of one order next to each other, so that the blocks resident
+  // on an SM at a time mostly run the same order's code (the kernels switch
+  // on p per block); within an order, larger problems first
+  std::vector<int> order(b->m.size());
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    if (b->m[x]->p != b->m[y]->p) return b->m[x]->p < b->m[y]->p;
+    return b->m[x]->K > b->m[y]->K;
+  });
   std::vector<int> e2p, e0, s2p, s0, l2p, l0;
-  block_maps(ke, b->blk, e2p, e0);
-  block_maps(ks, b->blk, s2p, s0);
-  block_maps(ke, 128, l2p, l0);
+  block_maps(ke, order, b->blk, e2p, e0);
+  block_maps(ks, order, b->blk, s2p, s0);
+  block_maps(ke, order, 128, l2p, l0);
   std::vector<int> all;
   size_t oe2p = 0, oe0 = oe2p + e2p.size(), os2p = oe0 + e0.size(), os0 = os2p + s2p.size(),
          ol2p = os0 + s0.size(), ol0 = ol2p + l2p.size();
