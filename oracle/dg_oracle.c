@@ -1,7 +1,7 @@
 /* dg_oracle.c -- CPU restatement of the reference RK-DG method (TEST ORACLE).
  *
  * This file is test infrastructure: only tests/, __graft_entry__.smoke()
- * and bench.py's CPU-baseline leg load it, as the checker and the timed CPU
+ * and bench.py's CPU-baseline leg load it, as the reference for results and the timed CPU
  * baseline.  The product never links it.
  *
  * It restates, as plain C loops over sides and elements in the reference's

@@ -1,6 +1,6 @@
 """ctypes wrapper and build recipe of the C oracle (dg_oracle.c).
 
-Test infrastructure only: the checker for the parity tests and the timed
+Test infrastructure only: the reference results of the parity tests and the timed
 CPU baseline of bench.py.  ``build()`` compiles dg_oracle.c with OpenMP into
 oracle/_build/liboracle.so.
 """
