@@ -68,3 +68,55 @@ def test_cli_runs_a_gmsh_file(dglib, tmp_path):
     vals = np.array([[float(x) for x in re.findall(r"\{([^}]*)\}", l)[0].split(",")]
                      for l in lines[1:1 + mesh.K]])
     np.testing.assert_allclose(vals, uv.T, rtol=0, atol=1e-12)
+
+
+def test_new_options_reject_bad_arguments(dglib, tmp_path):
+    """--field wants 4 numbers, --series t0 and whole (amp, omega, phase)
+    triples (at most 16), --reference-settings a known --problem."""
+    mesh = str(tmp_path / "none.pmsh")
+    for args in (["--field", "1,2,3"], ["--series", "0.5,1,2"],
+                 ["--series", ",".join(["1"] * 50)], ["--reference-settings"],
+                 ["--reference-settings", "--problem", "no_such_problem"]):
+        r = subprocess.run([CLI, "-n", "1", "-t", "1"] + args + [mesh], capture_output=True,
+                           text=True)
+        assert r.returncode == 1 and "Usage: dgcuda" in r.stdout, args
+
+
+def _pos_values(path, K):
+    lines = open(path).read().splitlines()
+    return np.array([[float(x) for x in re.findall(r"\{([^}]*)\}", l)[0].split(",")]
+                     for l in lines[1:1 + K]])
+
+
+@pytest.mark.gpu
+def test_cli_reference_settings_and_field(dglib, tmp_path):
+    """--reference-settings takes the problem file's settings (here spin:
+    its rotation, RK2, no limiter); --field replaces the velocity; both as
+    the library runs them."""
+    dg = dglib
+    mesh = dg.Mesh.square(12, 12, jitter=0.1, seed=8, bc=(-3, -3, -3, -3))
+    path = str(tmp_path / "m.pmsh")
+    mesh.write(path)
+    out = str(tmp_path / "a")
+    r = subprocess.run([CLI, "-n", "2", "-t", "6", "--eq", "advection", "--problem", "adv_spin",
+                        "--reference-settings", "-o", out, path], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    P, scheme = dg.params_for_problem("adv_spin")
+    assert scheme == dg.RK2
+    P.cfl = 0.7  # the CLI's default CFL for RK2
+    s = dg.Solver(mesh, dg.ADVECTION, 2, params=P)
+    s.init_conditions()
+    s.step(6, scheme, 0.0)
+    np.testing.assert_allclose(_pos_values(os.path.join(out, "U0-final.pos"), mesh.K),
+                               s.eval_u(0).T, rtol=0, atol=1e-12)
+    out = str(tmp_path / "b")
+    r = subprocess.run([CLI, "-n", "1", "-t", "6", "--eq", "advection", "--problem", "adv_sine",
+                        "--velocity", "0.3,-0.2", "--field", "0.1,-1.5,1.5,0.2", "-o", out, path],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    s = dg.Solver(mesh, dg.ADVECTION, 1, problem="adv_sine", cfl=0.5)
+    s.set_velocity_field(0.3, -0.2, (0.1, -1.5, 1.5, 0.2))
+    s.init_conditions()
+    s.step(6, dg.RK4, 0.0)
+    np.testing.assert_allclose(_pos_values(os.path.join(out, "U0-final.pos"), mesh.K),
+                               s.eval_u(0).T, rtol=0, atol=1e-12)
