@@ -780,6 +780,23 @@ __global__ void __launch_bounds__(kMaxBlock)
   }
 }
 
+// the same over the blocks [b_lo, b_lo + gridDim.x) of problems of one order
+// P (the block map lists the problems by order): each order gets its own
+// register allocation instead of the largest body's
+template <class Eq, int P>
+__global__ void __launch_bounds__(kMaxBlock)
+    k_element_batch_p(const __grid_constant__ Tab<P> tab, const BatchProb *__restrict__ probs,
+                      const int *__restrict__ blk2prob, const int *__restrict__ blk0, int b_lo,
+                      int stage, int check) {
+  const int b = b_lo + (int)blockIdx.x;
+  const int pi = blk2prob[b];
+  const BatchProb &pr = probs[pi];
+  const int e = (b - blk0[pi]) * blockDim.x + threadIdx.x;
+  if (e >= pr.K) return;
+  const ElemArgs a = batch_elem_args(pr, stage, check);
+  element_body<Eq, P, true>(tab, pr.q, a, e);
+}
+
 template <class Eq>
 __global__ void __launch_bounds__(kMaxBlock)
     k_face_batch(const __grid_constant__ BatchTabs tb, const BatchProb *__restrict__ probs,
@@ -981,8 +998,26 @@ struct Launch {
                                                    tcoef);
   }
   static void b_element(const BatchLaunch &b, int stage) {
-    k_element_batch<Eq><<<b.neblk, b.blk, 0, b.st>>>(btabs(b), b.probs, b.eblk2prob, b.eblk0,
-                                                      stage, b.limiter ? 0 : 1);
+    const BatchTabs &tb = btabs(b);
+    const int check = b.limiter ? 0 : 1;
+    if (b.eblk_p[4] == b.neblk) {  // blocks grouped by order: one launch per order
+      for (int p = 1; p <= 3; p++) {
+        const int lo = b.eblk_p[p], n = b.eblk_p[p + 1] - lo;
+        if (n <= 0) continue;
+        if (p == 1)
+          k_element_batch_p<Eq, 1><<<n, b.blk, 0, b.st>>>(tb.t1, b.probs, b.eblk2prob, b.eblk0,
+                                                            lo, stage, check);
+        else if (p == 2)
+          k_element_batch_p<Eq, 2><<<n, b.blk, 0, b.st>>>(tb.t2, b.probs, b.eblk2prob, b.eblk0,
+                                                            lo, stage, check);
+        else
+          k_element_batch_p<Eq, 3><<<n, b.blk, 0, b.st>>>(tb.t3, b.probs, b.eblk2prob, b.eblk0,
+                                                            lo, stage, check);
+      }
+    } else {
+      k_element_batch<Eq><<<b.neblk, b.blk, 0, b.st>>>(tb, b.probs, b.eblk2prob, b.eblk0, stage,
+                                                        check);
+    }
   }
   static void b_limit_tr(const BatchLaunch &b, int stage) {
     k_limit_tr_batch<Eq><<<b.neblk, b.blk, 0, b.st>>>(btabs(b), b.probs, b.eblk2prob, b.eblk0,
