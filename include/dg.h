@@ -209,7 +209,9 @@ dg_status dg_eval_vertices_view(dg_solver *s, int var, int view, double t, doubl
  * flux and the CFL wave speed take it at each point, the wave speed of an
  * element at its middle quadrature point (eval_global_lambda,
  * advection.cu:157-183).  Advection only (else DG_UNSUPPORTED).  The
- * rotating problems set their rotation when the solver is created. */
+ * rotating problems set their rotation when the solver is created; the
+ * exact solutions of the translating problems (adv_sine, adv_linear,
+ * adv_squarehill) move with (ax, ay) and do not follow grad. */
 dg_status dg_set_velocity_field(dg_solver *s, double ax, double ay, const double *grad);
 /* out[0..1] = (ax, ay), out[2..5] = grad, out[6] = the CFL wave speed */
 dg_status dg_get_velocity_field(const dg_solver *s, double out[7]);
