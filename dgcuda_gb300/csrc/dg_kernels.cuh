@@ -763,26 +763,9 @@ __device__ __forceinline__ ElemArgs batch_elem_args(const BatchProb &pr, int sta
   return a;
 }
 
-template <class Eq>
-__global__ void __launch_bounds__(kMaxBlock)
-    k_element_batch(const __grid_constant__ BatchTabs tb, const BatchProb *__restrict__ probs,
-                    const int *__restrict__ blk2prob, const int *__restrict__ blk0, int stage,
-                    int check) {
-  const int pi = blk2prob[blockIdx.x];
-  const BatchProb &pr = probs[pi];
-  const int e = (blockIdx.x - blk0[pi]) * blockDim.x + threadIdx.x;
-  if (e >= pr.K) return;
-  const ElemArgs a = batch_elem_args(pr, stage, check);
-  switch (pr.p) {
-    case 1: element_body<Eq, 1, true>(tb.t1, pr.q, a, e); break;
-    case 2: element_body<Eq, 2, true>(tb.t2, pr.q, a, e); break;
-    case 3: element_body<Eq, 3, true>(tb.t3, pr.q, a, e); break;
-  }
-}
-
-// the same over the blocks [b_lo, b_lo + gridDim.x) of problems of one order
-// P (the block map lists the problems by order): each order gets its own
-// register allocation instead of the largest body's
+// the fused element stage of a batch, over the blocks [b_lo, b_lo +
+// gridDim.x) of the problems of one order P (the block map lists the
+// problems by order): one launch per order, each at its own register count
 template <class Eq, int P>
 __global__ void __launch_bounds__(kMaxBlock)
     k_element_batch_p(const __grid_constant__ Tab<P> tab, const BatchProb *__restrict__ probs,
@@ -1000,23 +983,18 @@ struct Launch {
   static void b_element(const BatchLaunch &b, int stage) {
     const BatchTabs &tb = btabs(b);
     const int check = b.limiter ? 0 : 1;
-    if (b.eblk_p[4] == b.neblk) {  // blocks grouped by order: one launch per order
-      for (int p = 1; p <= 3; p++) {
-        const int lo = b.eblk_p[p], n = b.eblk_p[p + 1] - lo;
-        if (n <= 0) continue;
-        if (p == 1)
-          k_element_batch_p<Eq, 1><<<n, b.blk, 0, b.st>>>(tb.t1, b.probs, b.eblk2prob, b.eblk0,
-                                                            lo, stage, check);
-        else if (p == 2)
-          k_element_batch_p<Eq, 2><<<n, b.blk, 0, b.st>>>(tb.t2, b.probs, b.eblk2prob, b.eblk0,
-                                                            lo, stage, check);
-        else
-          k_element_batch_p<Eq, 3><<<n, b.blk, 0, b.st>>>(tb.t3, b.probs, b.eblk2prob, b.eblk0,
-                                                            lo, stage, check);
-      }
-    } else {
-      k_element_batch<Eq><<<b.neblk, b.blk, 0, b.st>>>(tb, b.probs, b.eblk2prob, b.eblk0, stage,
-                                                        check);
+    for (int p = 1; p <= 3; p++) {  // the blocks are grouped by order
+      const int lo = b.eblk_p[p], n = b.eblk_p[p + 1] - lo;
+      if (n <= 0) continue;
+      if (p == 1)
+        k_element_batch_p<Eq, 1><<<n, b.blk, 0, b.st>>>(tb.t1, b.probs, b.eblk2prob, b.eblk0, lo,
+                                                          stage, check);
+      else if (p == 2)
+        k_element_batch_p<Eq, 2><<<n, b.blk, 0, b.st>>>(tb.t2, b.probs, b.eblk2prob, b.eblk0, lo,
+                                                          stage, check);
+      else
+        k_element_batch_p<Eq, 3><<<n, b.blk, 0, b.st>>>(tb.t3, b.probs, b.eblk2prob, b.eblk0, lo,
+                                                          stage, check);
     }
   }
   static void b_limit_tr(const BatchLaunch &b, int stage) {

@@ -91,9 +91,9 @@ struct BatchLaunch {
   const int *sblk2prob = nullptr, *sblk0 = nullptr;  // side blocks of size blk
   const int *lblk2prob = nullptr, *lblk0 = nullptr;  // element blocks of 128 (wave speed)
   int neblk = 0, nsblk = 0, nlblk = 0;
-  // element blocks of order p are [eblk_p[p], eblk_p[p + 1]) when the map
-  // lists the problems by order (eblk_p[4] == neblk), p = 1..3
-  int eblk_p[5] = {0, 0, 0, 0, -1};
+  // element blocks of order p are [eblk_p[p], eblk_p[p + 1]), p = 1..3 (the
+  // map lists the problems by order)
+  int eblk_p[5] = {0, 0, 0, 0, 0};
 };
 
 struct BatchOps {

@@ -1129,17 +1129,14 @@ dg_status batch_build_maps(dg_batch *b) {
   L.neblk = (int)e2p.size();
   L.nsblk = (int)s2p.size();
   L.nlblk = (int)l2p.size();
-  // element-block ranges of orders 1..3 (contiguous: `order` sorts by p)
+  // element-block ranges of orders 1..3 (contiguous: `order` sorts by p;
+  // batch creation admits p = 1..3 only)
   int cnt[4] = {0, 0, 0, 0};
-  bool orders_ok = true;
-  for (auto *sv : b->m) {
-    if (sv->p < 1 || sv->p > 3) orders_ok = false;
-    else cnt[sv->p] += (sv->K + b->blk - 1) / b->blk;
-  }
+  for (auto *sv : b->m) cnt[sv->p] += (sv->K + b->blk - 1) / b->blk;
   L.eblk_p[1] = 0;
   L.eblk_p[2] = cnt[1];
   L.eblk_p[3] = cnt[1] + cnt[2];
-  L.eblk_p[4] = orders_ok ? cnt[1] + cnt[2] + cnt[3] : -1;
+  L.eblk_p[4] = cnt[1] + cnt[2] + cnt[3];
   L.blk = b->blk;
   if (b->graph) cudaGraphExecDestroy(b->graph);
   b->graph = nullptr;
