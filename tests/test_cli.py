@@ -120,3 +120,15 @@ def test_cli_reference_settings_and_field(dglib, tmp_path):
     s.step(6, dg.RK4, 0.0)
     np.testing.assert_allclose(_pos_values(os.path.join(out, "U0-final.pos"), mesh.K),
                                s.eval_u(0).T, rtol=0, atol=1e-12)
+
+
+def test_new_options_are_accepted(dglib, tmp_path):
+    """Well-formed --reference-settings, --field and --series pass the
+    argument checks (the run then stops at the missing mesh)."""
+    mesh = str(tmp_path / "none.pmsh")
+    for args in (["--problem", "adv_spin", "--reference-settings", "--eq", "advection"],
+                 ["--eq", "advection", "--problem", "adv_sine", "--field", "0,-1,1,0"],
+                 ["--problem", "euler_pulse", "--series", "0.9,0.05,4.4,2.9,0.03,8.9,2.6"]):
+        r = subprocess.run([CLI, "-n", "1", "-t", "1"] + args + [mesh], capture_output=True,
+                           text=True)
+        assert r.returncode == 1 and "mesh file not found" in r.stderr, (args, r.stdout)
