@@ -36,6 +36,8 @@ sys.path.insert(0, ROOT)
 METRIC = "DOF-stage updates/s at p=1..4 vs HBM roofline; batched/plain and adjoint/fwd ratio"
 UNIT = "DOF-stage/s"
 GAMMA = 1.4
+EQ_EULER, PB_RIEMANN4 = 1, 4  # dg_equation / dg_problem values (include/dg.h)
+REF_CAP_S = 120.0  # the reference arm's timed steps stop after this many seconds
 
 
 def workload_config(n, p, steps_note):
@@ -123,29 +125,33 @@ def reduce_replicas(units, seconds, dist=None):
     return float(u.item()) / float(t.item()), float(t.item())
 
 
-def cpu_baseline(n_sample, p, steps, threads=None):
-    """The oracle (C restatement of the reference method, OpenMP) on a
-    bounded sample of the workload: n_sample^2 squares, `steps` SSP-RK3
-    steps, all host threads."""
-    import dgcuda_gb300 as dg
+def oracle_workload(n, p):
+    """The oracle (the C restatement of the reference method, OpenMP) set up
+    on the bench's own mesh, built by the oracle's mesher (the same arrays as
+    the library's), with the bench problem's initial state: no product code
+    is loaded."""
     from oracle import oracle as orc
+    V, es, sxy, se = orc.mesh_square(n, n, jitter=0.1, seed=3, bc=(-4, -4, -4, -4))
+    o = orc.Oracle(EQ_EULER, p, V, es, sxy, se, orc.prm_vec(gamma=GAMMA), PB_RIEMANN4)
+    return orc, o, o.init()
+
+
+def cpu_baseline(n, p, steps, threads=None):
+    """The oracle on a bounded sample of the workload: `steps` SSP-RK3 steps
+    of the full mesh, all host threads."""
+    orc, o, c = oracle_workload(n, p)
     if threads:
         orc.set_threads(threads)
-    mesh = dg.Mesh.square(n_sample, n_sample, jitter=0.1, seed=3, bc=(-4, -4, -4, -4))
-    o = orc.Oracle.from_mesh(mesh, dg.EULER, p, orc.prm_vec(gamma=GAMMA),
-                             dg.PROBLEMS["euler_riemann4"])
-    c = o.init()
-    c, _, _ = o.step(c, 1, 0, 1, 0.2)  # warm-up
+    c, _, _ = o.step(c, 1, 0, 1, 0.2)  # warm-up (and the initial limiter pass)
     t0 = time.perf_counter()
-    c, _, n = o.step(c, steps, 0, 1, 0.2)
+    c, _, done = o.step(c, steps, 0, 1, 0.2)
     dt = time.perf_counter() - t0
     npm = (p + 1) * (p + 2) // 2
     cores = orc.lib().or_max_threads()
-    return {"value": mesh.K * 4 * npm * 3 * n / dt, "unit": UNIT, "cores": cores, "kind": "port",
+    return {"value": o.K * 4 * npm * 3 * done / dt, "unit": UNIT, "cores": cores, "kind": "port",
             "seconds": dt,
-            "sample": "%d SSP-RK3 steps (limiter on) of the same problem on %dx%d squares "
-                      "(%d triangles), p=%d, C oracle with OpenMP" % (n, n_sample, n_sample,
-                                                                      mesh.K, p)}
+            "sample": "%d SSP-RK3 steps (limiter on) of the same problem on the same %dx%d mesh "
+                      "(%d triangles), p=%d, C oracle with OpenMP" % (done, n, n, o.K, p)}
 
 
 def ensemble_bench(device, nprob, steps, warmup, seed=4000):
@@ -308,35 +314,31 @@ def adjoint_bench(device, n=256, steps=2000, ckpt=50, nrec=64, nsamp=20, seed=5)
 
 
 def run_reference(args, rank):
+    """The reference method on the host cores: the oracle (the reference's
+    kernels restated in C, pinned bit for bit to them; the reference's own
+    GPU code is CUDA and its host build cannot travel) on the bench's own
+    mesh, one full SSP-RK3 step per timed step, all host threads.  Imports
+    nothing from the product package."""
     if rank != 0:
         return 0
-    n_sample = 512
-    cb = None
-    # each timed step is one SSP-RK3 step of the sampled mesh; the run is
-    # capped at ~90 s of CPU time
-    import dgcuda_gb300 as dg
-    from oracle import oracle as orc
-    mesh = dg.Mesh.square(n_sample, n_sample, jitter=0.1, seed=3, bc=(-4, -4, -4, -4))
-    o = orc.Oracle.from_mesh(mesh, dg.EULER, args.p, orc.prm_vec(gamma=GAMMA),
-                             dg.PROBLEMS["euler_riemann4"])
-    c = o.init()
-    for _ in range(args.warmup):
+    orc, o, c = oracle_workload(args.n, args.p)
+    for _ in range(min(args.warmup, 5)):
         c, _, _ = o.step(c, 1, 0, 1, 0.2)
     done, t0 = 0, time.perf_counter()
     while done < args.steps:
         c, _, _ = o.step(c, 1, 0, 1, 0.2)
         done += 1
-        if time.perf_counter() - t0 > 90:
+        if time.perf_counter() - t0 > REF_CAP_S:
             break
     dt = time.perf_counter() - t0
     npm = (args.p + 1) * (args.p + 2) // 2
-    value = mesh.K * 4 * npm * 3 * done / dt
+    value = o.K * 4 * npm * 3 * done / dt
     cores = orc.lib().or_max_threads()
     cb = {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-          "sample": "%d SSP-RK3 steps (limiter on) of the same problem on %dx%d squares (%d "
-                    "triangles), p=%d; the reference's CUDA cannot run on this CPU, so its "
-                    "method restated in C (oracle/dg_oracle.c, pinned bit-exact to the "
-                    "reference's kernels) runs with OpenMP" % (done, n_sample, n_sample, mesh.K,
+          "sample": "%d SSP-RK3 steps (limiter on) of the bench problem on the same %dx%d mesh "
+                    "(%d triangles), p=%d; the reference's CUDA cannot run on these cores, so "
+                    "its method restated in C (oracle/dg_oracle.c, pinned bit for bit to the "
+                    "reference's kernels) runs with OpenMP" % (done, args.n, args.n, o.K,
                                                                args.p)}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": done,
             "warmup": args.warmup, "ms_per_step": dt / done * 1e3, "higher_is_better": True,
@@ -508,7 +510,7 @@ def main():
 
     cb = None
     if rank == 0 and not args.no_cpu:
-        cb = cpu_baseline(512, p, 3)
+        cb = cpu_baseline(n, p, 4)
 
     if rank == 0:
         clocks = summarize_clocks(clk_lines)

@@ -43,7 +43,8 @@ def _headers():
 def _compile(src, flags):
     obj = os.path.join(BUILD, src + ".o")
     path = os.path.join(CSRC, src)
-    newest = max([os.path.getmtime(path)] + [os.path.getmtime(h) for h in _headers()])
+    newest = max([os.path.getmtime(path), os.path.getmtime(__file__)] +
+                 [os.path.getmtime(h) for h in _headers()])
     if os.path.exists(obj) and os.path.getmtime(obj) >= newest:
         return obj
     cmd = [nvcc()] + ARCH + flags + ["-c", path, "-o", obj]
@@ -55,7 +56,10 @@ def _compile(src, flags):
 
 def build(verbose=False, jobs=None):
     os.makedirs(BUILD, exist_ok=True)
-    common = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "-I" + CSRC,
+    # host code: no contraction of a*b+c into FMAs the source does not write,
+    # so meshes and geometry have the same bits on x86 and Arm
+    common = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
+              "-I" + CSRC,
               "-I" + os.path.join(ROOT, "include")]
     cuflags = common + ["-Xptxas", "-O3", "--expt-relaxed-constexpr"]
     srcs = _sources()

@@ -9,16 +9,24 @@
 // Who needs this: code that may not allocate device memory at the moment it
 // evaluates the operator -- a host application that hands this library a
 // fixed memory budget up front and forbids allocation afterwards (device
-// memory owned by its own pool), a latency-critical loop where a cudaMalloc
-// would synchronise the device and stall every stream, or a caller running
-// under a CUDA stream capture, where cudaMalloc is not permitted.
+// memory owned by its own pool), or a latency-critical loop where a
+// cudaMalloc would synchronise the device and stall every stream.
+//
+// The call runs on the solver's stream (dg_solver_stream) and returns once
+// that stream has finished its work: the caller's input must be ready with
+// respect to that stream when the call is made.
 //
 // Limits: the array holds DG_NOALLOC_SCRATCH_BYTES (32 MiB) on every GPU that
 // loads the library, for the life of the process; problems whose working set
 // exceeds it are rejected with DG_UNSUPPORTED.  All calls share the one
 // array, so calls whose work overlaps on the GPU (different streams or
 // threads without ordering) race on it.  Every call overwrites all of the
-// scratch it reads, so nothing carries over from the previous call.
+// scratch it reads, so nothing carries over from the previous call.  The
+// first call on a device looks up the array's device address and keeps it
+// for the life of the process (make that first call before any stream
+// capture); after cudaDeviceReset, or any teardown of the device's primary
+// context, the kept address is stale and the entry point must not be called
+// again in that process.
 #include <cuda_runtime.h>
 
 #include <mutex>

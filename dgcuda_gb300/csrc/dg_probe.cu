@@ -6,6 +6,7 @@
 
 #include "dg_device.cuh"
 #include "dg_internal.h"
+#include "../../include/dg_test.h"
 
 namespace {
 __global__ void k_fma64(double *out, int iters, double a, double b) {

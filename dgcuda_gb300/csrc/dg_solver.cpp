@@ -159,12 +159,19 @@ void collect_profile(dg_solver *s) {
 
 enum { K_TRACE = 0, K_FACE = 1, K_ELEMENT = 2, K_LIMIT = 3, K_CFL = 4, K_RK = 5 };
 
-// one RK stage of the DG operator: out = ca*un + cb*us + cc*dt*L(us)
+// one RK stage of the DG operator: out = ca*un + cb*us + cc*dt*L(us).
+// With the tensor-core contractions on, the element stage is the one the
+// fused SSP-RK3 step runs (k_element_oz; the traces of `out` it also leaves
+// in T are not used, and no positivity rule is applied to them), so dg_rhs
+// and the RK4 / RK2 loops evaluate the operator the SSP-RK3 step evaluates.
 void stage(dg_solver *s, double *us, const double *un, double *out, double ca, double cb,
            double cc, double tcoef, const double *dtp) {
   run(s, K_TRACE, [&] { s->ops->trace(s->ctx, us); });
   run(s, K_FACE, [&] { s->ops->face(s->ctx, &s->ds->t, tcoef); });
-  run(s, K_ELEMENT, [&] { s->ops->element(s->ctx, us, un, out, ca, cb, cc, dtp); });
+  if (s->ctx.oz)
+    run(s, K_ELEMENT, [&] { s->ops->element_tr(s->ctx, us, un, out, ca, cb, cc, dtp, 0); });
+  else
+    run(s, K_ELEMENT, [&] { s->ops->element(s->ctx, us, un, out, ca, cb, cc, dtp); });
 }
 
 void limit(dg_solver *s, double *u) {

@@ -325,32 +325,22 @@ long long dg_kernel_launches(const dg_solver *s);
 
 /* du/dt like dg_rhs, for callers that may not allocate device memory while
  * evaluating it (an application that owns all device memory and forbids
- * allocation after set-up, a latency-critical loop, a stream capture).
- * C_device and dCdt_device are the caller's device buffers in the reference
- * layout; all working memory comes from a static 32 MiB array that every GPU
- * loading the library holds until exit.  Larger problems get DG_UNSUPPORTED.
- * The first call on a device looks up that array's address (make it before
- * any stream capture).  Calls that overlap on the GPU race on the array.
- * No counterpart in the reference. */
+ * allocation after set-up, or a latency-critical loop where a cudaMalloc
+ * would synchronise the device).  C_device and dCdt_device are the caller's
+ * device buffers in the reference layout, ready with respect to the
+ * solver's stream; the call returns when that stream has finished.  All
+ * working memory comes from a static 32 MiB array that every GPU loading the
+ * library holds until exit.  Larger problems get DG_UNSUPPORTED.  The first
+ * call on a device looks up that array's address and keeps it (make it
+ * before any stream capture; after cudaDeviceReset the kept address is
+ * stale).  Calls that overlap on the GPU race on the array.  No counterpart
+ * in the reference. */
 dg_status dg_rhs_device_noalloc(dg_solver *s, double t, const double *C_device,
                                 double *dCdt_device);
 
 /* FP64 FMA throughput of `device` in TFLOP/s (the binding roof of the DG
  * kernels on GB300), timed with CUDA events; no reference counterpart */
 dg_status dg_measure_fp64_peak(int device, double *tflops);
-/* the reciprocal the flux kernels use (Newton-Raphson from the hardware's
- * approximate reciprocal) and IEEE division, on the device, for n host
- * values: r[i] = rcp(x[i]), q[i] = 1 / x[i] (a check of the former) */
-dg_status dg_probe_reciprocal(int device, int n, const double *x, double *r, double *q);
-/* the sound speed's square root and IEEE sqrt on the device: r[i] =
- * sqrt_pos(x[i]), q[i] = sqrt(x[i]) (checks) */
-dg_status dg_probe_sqrt(int device, int n, const double *x, double *r, double *q);
-/* the Euler positivity test (rho >= 0, p >= 0) on the device for n states
- * U[4i..4i+3] = (rho, m_x, m_y, E): fast[i] = 1 where its single-precision
- * filter settles the state as physical, exact[i] = 1 where the FP64 test
- * finds it physical (fast implies exact; checks of the filter) */
-dg_status dg_probe_physical(int device, int n, const double *U, int *fast, int *exact);
-
 #ifdef __cplusplus
 }
 #endif

@@ -1069,3 +1069,153 @@ int or_l2err(or_solver *o, const double *C, double t, double *err2) {
   }
   return 0;
 }
+
+/* ---------------- synthetic square meshes ----------------
+ * The jittered square-split meshes of the benchmark configurations, built
+ * without the product library (bench.py's reference arm times the oracle on
+ * the same mesh the GPU runs).  Same construction, numbering and rounding as
+ * the library's dg_mesh_square: nx x ny squares on [x0,x1]x[y0,y1], each cut
+ * along its (0,0)-(1,1) diagonal into two CCW triangles; interior vertices
+ * jittered by (2u - 1) jitter h with u from splitmix64(seed), x then y, row by
+ * row; sides in first-visit order (element by element, faces 0, 1, 2; face k
+ * joins vertices k and k+1, the .pmsh convention of genmesh.py), left = the
+ * first element to visit a side; then boundary sides first by code -1..-4
+ * (stable), interior sides after them.  bc = {left, right, bottom, top}: 0 is
+ * periodic (paired), else a boundary code.  Arrays in .pmsh column order:
+ * V[6][K], es[3][K], sxy[4][S], se[4][S].  tests/test_oracle_mesh.py checks
+ * that the arrays equal the library's bit for bit. */
+static unsigned long long sm64(unsigned long long *s) {
+  unsigned long long z = (*s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+static double unif01(unsigned long long *s) { return (double)(sm64(s) >> 11) * 0x1.0p-53; }
+
+int or_mesh_square_sizes(int nx, int ny, const int *bc, int *K, int *S) {
+  const int px = bc[0] == 0, py = bc[2] == 0;
+  if (nx < 1 || ny < 1) return 1;
+  *K = 2 * nx * ny;
+  *S = 3 * nx * ny + (px ? 0 : ny) + (py ? 0 : nx);
+  return 0;
+}
+
+typedef struct {
+  double x1, y1, x2, y2;
+  int left, right, lsn, rsn, box;
+} or_tmp_side;
+
+int or_mesh_square(int nx, int ny, double x0, double x1, double y0, double y1, double jitter,
+                   unsigned long long seed, const int *bc, double *V, int *es, double *sxy,
+                   int *se) {
+  const int px = bc[0] == 0 || bc[1] == 0, py = bc[2] == 0 || bc[3] == 0;
+  int K, Sx;
+  if ((bc[0] == 0) != (bc[1] == 0) || (bc[2] == 0) != (bc[3] == 0)) return 1;
+  if (or_mesh_square_sizes(nx, ny, bc, &K, &Sx)) return 1;
+  const double hx = (x1 - x0) / nx, hy = (y1 - y0) / ny;
+  const int vx = nx + 1, vy = ny + 1;
+  const unsigned long long nv = (unsigned long long)vx * vy;
+  double *X = (double *)xmalloc(sizeof(double) * nv), *Y = (double *)xmalloc(sizeof(double) * nv);
+  unsigned long long st = seed;
+  for (int j = 0; j < vy; j++)
+    for (int i = 0; i < vx; i++) {
+      double x = x0 + i * hx, y = y0 + j * hy;
+      if (i > 0 && i < nx && j > 0 && j < ny) {
+        double ux = unif01(&st), uy = unif01(&st);
+        x += (2 * ux - 1) * jitter * hx;
+        y += (2 * uy - 1) * jitter * hy;
+      }
+      X[(size_t)j * vx + i] = x;
+      Y[(size_t)j * vx + i] = y;
+    }
+  /* open-addressing table: side key -> side index */
+  size_t cap = 1;
+  while (cap < (size_t)2 * Sx + 16) cap <<= 1;
+  unsigned long long *keys = (unsigned long long *)xmalloc(sizeof(unsigned long long) * cap);
+  int *vals = (int *)xmalloc(sizeof(int) * cap);
+  or_tmp_side *sd = (or_tmp_side *)xmalloc(sizeof(or_tmp_side) * (size_t)Sx);
+  int ns = 0, e = 0, rc = 0;
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) {
+      const int tri[2][3][2] = {{{i, j}, {i + 1, j}, {i + 1, j + 1}},
+                                {{i, j}, {i + 1, j + 1}, {i, j + 1}}};
+      for (int t = 0; t < 2; t++, e++) {
+        for (int k = 0; k < 3; k++) {
+          size_t gv = (size_t)tri[t][k][1] * vx + tri[t][k][0];
+          V[(size_t)(2 * k) * K + e] = X[gv];
+          V[(size_t)(2 * k + 1) * K + e] = Y[gv];
+        }
+        for (int k = 0; k < 3; k++) {
+          const int a = k, b = (k + 1) % 3;
+          const int ia = tri[t][a][0], ja = tri[t][a][1], ib = tri[t][b][0], jb = tri[t][b][1];
+          long long ka = (long long)(py ? ja % ny : ja) * vx + (px ? ia % nx : ia);
+          long long kb = (long long)(py ? jb % ny : jb) * vx + (px ? ib % nx : ib);
+          const unsigned long long key =
+              (unsigned long long)(ka < kb ? ka : kb) * nv + (unsigned long long)(ka < kb ? kb : ka) + 1;
+          size_t h = (size_t)((key * 0x9E3779B97F4A7C15ull) >> 17) & (cap - 1);
+          while (keys[h] && keys[h] != key) h = (h + 1) & (cap - 1);
+          if (!keys[h]) {
+            if (ns >= Sx) { rc = 2; goto done; }
+            or_tmp_side *s = &sd[ns];
+            s->x1 = V[(size_t)(2 * a) * K + e];
+            s->y1 = V[(size_t)(2 * a + 1) * K + e];
+            s->x2 = V[(size_t)(2 * b) * K + e];
+            s->y2 = V[(size_t)(2 * b + 1) * K + e];
+            s->left = e;
+            s->lsn = k;
+            s->right = -1;
+            s->rsn = 0;
+            s->box = -1;
+            if (ia == 0 && ib == 0) s->box = 0;
+            else if (ia == nx && ib == nx) s->box = 1;
+            else if (ja == 0 && jb == 0) s->box = 2;
+            else if (ja == ny && jb == ny) s->box = 3;
+            if (s->box >= 0 && bc[s->box] == 0) s->box = -1;
+            keys[h] = key;
+            vals[h] = ns;
+            es[(size_t)k * K + e] = ns++;
+          } else {
+            or_tmp_side *s = &sd[vals[h]];
+            s->right = e;
+            s->rsn = k;
+            es[(size_t)k * K + e] = vals[h];
+          }
+        }
+      }
+    }
+  if (ns != Sx) { rc = 2; goto done; }
+  for (int n = 0; n < ns; n++)
+    if (sd[n].right < 0) {
+      if (sd[n].box < 0) { rc = 3; goto done; }
+      sd[n].right = bc[sd[n].box];
+    }
+  {
+    /* stable order: codes -1, -2, -3, -4, then interior sides */
+    int *newidx = (int *)xmalloc(sizeof(int) * (size_t)ns);
+    int pos = 0;
+    for (int rank = 1; rank <= 5; rank++)
+      for (int n = 0; n < ns; n++) {
+        const int r = sd[n].right < 0 ? -sd[n].right : 5;
+        if (r != rank) continue;
+        newidx[n] = pos;
+        sxy[pos] = sd[n].x1;
+        sxy[(size_t)ns + pos] = sd[n].y1;
+        sxy[2 * (size_t)ns + pos] = sd[n].x2;
+        sxy[3 * (size_t)ns + pos] = sd[n].y2;
+        se[pos] = sd[n].left;
+        se[(size_t)ns + pos] = sd[n].right;
+        se[2 * (size_t)ns + pos] = sd[n].lsn;
+        se[3 * (size_t)ns + pos] = sd[n].rsn;
+        pos++;
+      }
+    for (size_t q = 0; q < (size_t)3 * K; q++) es[q] = newidx[es[q]];
+    free(newidx);
+  }
+done:
+  free(X);
+  free(Y);
+  free(keys);
+  free(vals);
+  free(sd);
+  return rc;
+}

@@ -26,7 +26,9 @@ def build():
     if os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
         return LIB
     cc = shutil.which("gcc") or "cc"
-    cmd = [cc, "-O2", "-fopenmp", "-shared", "-fPIC", SRC, "-o", LIB, "-lm"]
+    # no contraction of a*b+c into FMAs the source does not write: the same
+    # bits on x86 and Arm
+    cmd = [cc, "-O2", "-ffp-contract=off", "-fopenmp", "-shared", "-fPIC", SRC, "-o", LIB, "-lm"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + r.stderr)
@@ -60,6 +62,10 @@ def lib():
         L.or_flattened.argtypes = [C.c_void_p]
         L.or_set_threads.argtypes = [C.c_int]
         L.or_get_tables.argtypes = [C.c_void_p, _dp]
+        L.or_mesh_square_sizes.argtypes = [C.c_int, C.c_int, _ip, _ip, _ip]
+        L.or_mesh_square.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                     C.c_double, C.c_double, C.c_ulonglong, _ip, _dp, _ip, _dp,
+                                     _ip]
         L.or_set_bathymetry.argtypes = [C.c_void_p, _dp]
         L.or_set_field.argtypes = [C.c_void_p, C.c_double, C.c_double, _dp]
         L.or_set_series.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp, C.c_double]
@@ -195,6 +201,27 @@ class Oracle:
         if getattr(self, "h", None):
             self.L.or_destroy(self.h)
             self.h = None
+
+
+def mesh_square(nx, ny, box=(0.0, 1.0, 0.0, 1.0), jitter=0.0, seed=0, bc=(0, 0, 0, 0)):
+    """The jittered square-split mesh of the benchmark configurations, built
+    by the oracle (same arrays as the library's dg_mesh_square): V[6,K],
+    elem_sides[3,K], side_xy[4,S], side_elems[4,S] in .pmsh column order."""
+    L = lib()
+    b = np.ascontiguousarray(bc, dtype=np.int32)
+    K, S = C.c_int(), C.c_int()
+    if L.or_mesh_square_sizes(nx, ny, b.ctypes.data_as(_ip), C.byref(K), C.byref(S)):
+        raise ValueError("bad mesh size")
+    V = np.empty((6, K.value))
+    es = np.empty((3, K.value), dtype=np.int32)
+    sxy = np.empty((4, S.value))
+    se = np.empty((4, S.value), dtype=np.int32)
+    rc = L.or_mesh_square(nx, ny, box[0], box[1], box[2], box[3], jitter, seed,
+                          b.ctypes.data_as(_ip), _d(V), es.ctypes.data_as(_ip), _d(sxy),
+                          se.ctypes.data_as(_ip))
+    if rc:
+        raise ValueError("or_mesh_square failed (%d)" % rc)
+    return V, es, sxy, se
 
 
 def set_threads(n):

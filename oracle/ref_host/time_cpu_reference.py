@@ -17,7 +17,10 @@ import time
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+sys.path.insert(0, ROOT)
+from oracle.reference_tree import reference_root  # noqa: E402
+
+REF = sys.argv[1] if len(sys.argv) > 1 else reference_root()
 STEPS = int(sys.argv[2]) if len(sys.argv) > 2 else 100
 MESH = os.path.join(REF, "src/2d/conservation/euler/supersonic/mesh/sv-large.pmsh")
 

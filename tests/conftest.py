@@ -9,7 +9,10 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 GOLDEN = os.path.join(ROOT, "tests", "golden")
-REF_TREE = "/root/reference/src/2d/conservation"
+from oracle.reference_tree import conservation_tree  # noqa: E402
+
+# the reference's src/2d/conservation tree where it is mounted, else None
+REF_TREE = conservation_tree()
 
 
 def pytest_configure(config):

@@ -22,6 +22,7 @@ Run from the repository root:  python tests/golden/make_golden.py
 import os
 import subprocess
 import sys
+import tempfile
 
 import numpy as np
 
@@ -29,9 +30,11 @@ ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)
 sys.path.insert(0, ROOT)
 import dgcuda_gb300 as dg  # noqa: E402
 
-REF_TREE = "/root/reference/src/2d/conservation"
+from oracle.reference_tree import conservation_tree, reference_root  # noqa: E402
+
+REF_TREE = conservation_tree()
 OUT = os.path.join(ROOT, "tests", "golden")
-TMP = os.path.join(ROOT, "_work", "golden_tmp")
+TMP = tempfile.mkdtemp(prefix="dg_golden_")
 REF = os.path.join(ROOT, "oracle", "_ref")
 EQ_BIN = {dg.ADVECTION: "ref_advection", dg.EULER: "ref_euler",
           dg.SHALLOW_WATER: "ref_shallowwater", dg.MAXWELL: "ref_maxwells"}
@@ -39,7 +42,8 @@ PB = dg.PROBLEMS
 
 
 def build_ref():
-    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref_host")], check=True)
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref_host"),
+                    "REF_ROOT=" + reference_root()], check=True)
 
 
 def run_ref(eq, p, mode, problem, mesh, C, prm, nsteps=0, limiter=0, rk=4):

@@ -9,8 +9,8 @@ import pytest
 from conftest import ROOT
 
 
-def declared():
-    src = open(os.path.join(ROOT, "include", "dg.h")).read()
+def declared(header="dg.h"):
+    src = open(os.path.join(ROOT, "include", header)).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
     return sorted(set(re.findall(r"\b(dg_\w+)\s*\(", src)))
 
@@ -21,6 +21,16 @@ def test_every_declared_symbol_is_exported(dglib):
     assert len(names) >= 30
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
+
+
+def test_test_header_symbols_are_exported_and_kept_apart(dglib):
+    """The arithmetic checks live in include/dg_test.h, not in the drop-in
+    interface."""
+    lib = ctypes.CDLL(dglib.lib_path())
+    probes = declared("dg_test.h")
+    assert probes == ["dg_probe_physical", "dg_probe_reciprocal", "dg_probe_sqrt"]
+    assert not set(probes) & set(declared())
+    assert all(hasattr(lib, n) for n in probes)
 
 
 def test_version_and_defaults(dglib):

@@ -59,6 +59,30 @@ def test_rhs_exact_basis_matches_oracle(dglib, oracle_mod, name):
     assert relerr(s.eval_rhs(d["C"].reshape(s.shape), t), o.rhs(d["C"], t), s.N) <= RHS_TOL
 
 
+def _euler_tensor_goldens():
+    out = []
+    for name in golden_names("rhs_euler"):
+        p = int(load_golden(name)["p"])
+        if 1 <= p <= 4:
+            out.append(name)
+    return out
+
+
+@pytest.mark.parametrize("tensor", [True, False], ids=["tensor", "fp64"])
+@pytest.mark.parametrize("name", _euler_tensor_goldens())
+def test_euler_rhs_both_element_paths_match_reference(dglib, name, tensor):
+    """The element stage the bench times (basis contractions on the tensor
+    cores, k_element_oz, with its start-of-run traces k_trace_oz) and the
+    FP64-FMA one, each through dg_rhs, against the reference kernels'
+    right-hand side with the reference tabulation: 1e-12 norm-wise."""
+    d = load_golden(name)
+    s = solver_for(dglib, d)
+    s.tensor_contractions = tensor
+    assert s.tensor_contractions == tensor
+    r = s.eval_rhs(d["C"].reshape(s.shape), float(d["prm"][0]))
+    assert relerr(r, d["out"], s.N) <= RHS_TOL
+
+
 @pytest.mark.parametrize("name", golden_names("init_"))
 def test_projection_matches_reference(dglib, name):
     d = load_golden(name)

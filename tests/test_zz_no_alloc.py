@@ -1,6 +1,7 @@
 """dg_rhs_device_noalloc: the right-hand side for callers that may not
 allocate device memory during the call (a host application that owns all
-device memory, a latency-critical loop, a stream capture).  Its working
+device memory and forbids allocation after set-up, or a latency-critical
+loop where a cudaMalloc would synchronise the device).  Its working
 memory is a static array inside the library; the test checks, through the C
 ABI, that two calls in a row give dg_rhs's result within the right-hand-side
 tolerance of the other parity tests (1e-12, norm-wise per variable), and that
@@ -46,6 +47,9 @@ def test_noalloc_rhs_matches_dg_rhs_twice(dglib):
         ref = s.eval_rhs(c, 0.25)
         dev_in = torch.from_numpy(c).cuda()
         dev_out = torch.full_like(dev_in, float("nan"))
+        # the entry point works on the solver's own stream: the copy and the
+        # NaN fill above must be finished before it starts
+        torch.cuda.synchronize()
         rc = fn(s._h, 0.25, dev_in.data_ptr(), dev_out.data_ptr())
         assert rc == 0, dg.load_library().dg_last_error().decode()
         got = dev_out.cpu().numpy()
