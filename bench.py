@@ -419,7 +419,8 @@ def main():
     stop.set()
     th.join(timeout=10)
     launches = s.kernel_launches() - launches0
-    kern = {k: s.profile_get(k) for k in ("trace", "face", "element", "limit", "cfl", "rk")}
+    kern = {k: s.profile_get(k)
+            for k in ("trace", "face", "element", "limit", "means", "cfl", "rk")}
     s.profile(False)
     dof_stage = K * N * npm * 3 * args.steps
     value, sec = reduce_replicas(dof_stage, ms / 1e3, dist if world > 1 else None)
@@ -427,7 +428,7 @@ def main():
 
     # ---- roofline of the dominant kernel ----
     stage_ms = {k: v[1] / max(v[0], 1) for k, v in kern.items()}
-    dom = max(("trace", "face", "element", "limit"), key=lambda k: kern[k][1])
+    dom = max(("trace", "face", "element", "limit", "means"), key=lambda k: kern[k][1])
     elem_ms = stage_ms[dom]
     bpe = alg_bytes_per_elem(N, npm)
     achieved = K * bpe / (elem_ms / 1e3) / 1e9
@@ -445,7 +446,7 @@ def main():
             traffic = tr[key]["dram_bytes_per_element"] * K
     except (OSError, ValueError, KeyError):
         pass
-    stage_total_ms = sum(kern[k][1] for k in ("trace", "face", "element", "limit")) / (
+    stage_total_ms = sum(kern[k][1] for k in ("trace", "face", "element", "limit", "means")) / (
         3 * args.steps)
     fpe = alg_flops_per_elem(N, npm, nq, n1)
     fp64_achieved = K * fpe / (stage_total_ms / 1e3) / 1e12

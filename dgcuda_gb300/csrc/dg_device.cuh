@@ -129,12 +129,15 @@ DG_HD double rcp(double x) {
 #ifdef __CUDACC__
 // x to single precision from its high word alone, with integer instructions:
 // sign, exponent rebiased, the top 20 of the 52 fraction bits (relative
-// error below 2^-20); NaN when x is outside the normal float range (or zero)
+// error below 2^-20); a zero or denormal x (exponent field 0) becomes a zero
+// of its sign (off by less than 2^-1022: a denormal's square is far below
+// any margin the filter below relies on); NaN when x is outside the normal
+// float range otherwise
 __device__ __forceinline__ float f32_of_hi(double x) {
   const unsigned hi = (unsigned)__double2hiint(x);
   const unsigned ex = (hi >> 20) & 0x7FFu;
   const unsigned b = (hi & 0x80000000u) | ((ex - 896u) << 23) | ((hi & 0xFFFFFu) << 3);
-  return __uint_as_float(ex - 897u < 253u ? b : 0x7FC00000u);
+  return __uint_as_float(ex == 0u ? (hi & 0x80000000u) : ex - 897u < 253u ? b : 0x7FC00000u);
 }
 
 // true only if the Euler state U (rho, m_x, m_y, E) is physical (rho >= 0,

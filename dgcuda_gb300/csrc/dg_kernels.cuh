@@ -104,12 +104,42 @@ struct FaceArgs {
   const double *sgeo, *bxy;
   const double *vtx;  // element vertices (rows of Kp): edge-point positions of a velocity field
   double *Fh;
+  double *Fs;         // per side the sum over its edge points of Fh, [side][var] (FS kernels)
   const double *tptr, *dtp;
   double tcoef;
   int S, Sb, Kp;
 };
 
-template <class Eq, int P>
+// N contiguous doubles at p (16-byte aligned when N is even): 128-bit loads
+// and stores where N is even, scalar ones otherwise
+template <int N>
+__device__ __forceinline__ void load_vars(const double *p, double (&v)[N]) {
+  if constexpr (N % 2 == 0) {
+#pragma unroll
+    for (int k = 0; k < N / 2; k++) {
+      const double2 d = __ldg(reinterpret_cast<const double2 *>(p) + k);
+      v[2 * k] = d.x;
+      v[2 * k + 1] = d.y;
+    }
+  } else {
+#pragma unroll
+    for (int n = 0; n < N; n++) v[n] = p[n];
+  }
+}
+template <int N>
+__device__ __forceinline__ void store_vars(double *p, const double (&v)[N]) {
+  if constexpr (N % 2 == 0) {
+#pragma unroll
+    for (int k = 0; k < N / 2; k++)
+      reinterpret_cast<double2 *>(p)[k] = make_double2(v[2 * k], v[2 * k + 1]);
+  } else {
+#pragma unroll
+    for (int n = 0; n < N; n++) p[n] = v[n];
+  }
+}
+
+// FS: also store the per-side sums of the scaled fluxes in a.Fs
+template <class Eq, int P, bool FS = false>
 __device__ __forceinline__ void face_body(const Tab<P> &tab, const EqP &q, const FaceArgs &a,
                                           int s) {
   constexpr int N = Eq::N, N1 = P + 1;
@@ -118,16 +148,16 @@ __device__ __forceinline__ void face_body(const Tab<P> &tab, const EqP &q, const
   const double nx = a.sgeo[s], ny = a.sgeo[S + s], hl = a.sgeo[2 * (size_t)S + s];
   const double *TL = a.T + ((size_t)sd.x * 3 + sd.z) * (N1 * N);
   double *F = a.Fh + (size_t)s * (N1 * N);
+  double fs[N];
+#pragma unroll
+  for (int n = 0; n < N; n++) fs[n] = 0.0;
   if (sd.y >= 0) {
     const double *TR = a.T + ((size_t)sd.y * 3 + sd.w) * (N1 * N);
 #pragma unroll
     for (int j = 0; j < N1; j++) {
       double UL[N], UR[N], Fn[N];
-#pragma unroll
-      for (int n = 0; n < N; n++) {
-        UL[n] = TL[j * N + n];
-        UR[n] = TR[(N1 - 1 - j) * N + n];
-      }
+      load_vars<N>(TL + j * N, UL);
+      load_vars<N>(TR + (N1 - 1 - j) * N, UR);
       if constexpr (Eq::kField) {
         if (q.field) {  // the velocity at the edge point, on the left face
           const int va = sd.z, vb = sd.z == 2 ? 0 : sd.z + 1;
@@ -146,7 +176,11 @@ __device__ __forceinline__ void face_body(const Tab<P> &tab, const EqP &q, const
       }
       const double sc = hl * tab.w1[j] * Eq::kRawScale;  // exact: a power of two
 #pragma unroll
-      for (int n = 0; n < N; n++) F[j * N + n] = Fn[n] * sc;
+      for (int n = 0; n < N; n++) {
+        Fn[n] *= sc;
+        if (FS) fs[n] += Fn[n];
+      }
+      store_vars<N>(F + j * N, Fn);
     }
   } else {
     const double t = *a.tptr + a.tcoef * *a.dtp;
@@ -155,8 +189,7 @@ __device__ __forceinline__ void face_body(const Tab<P> &tab, const EqP &q, const
 #pragma unroll
     for (int j = 0; j < N1; j++) {
       double UL[N], UR[N], Fn[N];
-#pragma unroll
-      for (int n = 0; n < N; n++) UL[n] = TL[j * N + n];
+      load_vars<N>(TL + j * N, UL);
       const double r = 0.5 + 0.5 * tab.t1[j];
       const double px = fma(r, xb - xa, xa), py = fma(r, yb - ya, ya);
       ghost_state<Eq>(q, sd.y, UL, UR, px, py, t, nx, ny);
@@ -173,17 +206,22 @@ __device__ __forceinline__ void face_body(const Tab<P> &tab, const EqP &q, const
       }
       const double sc = hl * tab.w1[j] * Eq::kRawScale;  // exact: a power of two
 #pragma unroll
-      for (int n = 0; n < N; n++) F[j * N + n] = Fn[n] * sc;
+      for (int n = 0; n < N; n++) {
+        Fn[n] *= sc;
+        if (FS) fs[n] += Fn[n];
+      }
+      store_vars<N>(F + j * N, Fn);
     }
   }
+  if (FS) store_vars<N>(a.Fs + (size_t)s * N, fs);
 }
 
-template <class Eq, int P>
+template <class Eq, int P, bool FS = false>
 __global__ void __launch_bounds__(kMaxBlock) k_face(const __grid_constant__ Tab<P> tab,
                                                     const __grid_constant__ EqP q,
                                                     const __grid_constant__ FaceArgs a) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s < a.S) face_body<Eq, P>(tab, q, a, s);
+  if (s < a.S) face_body<Eq, P, FS>(tab, q, a, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -264,6 +302,8 @@ struct ElemArgs {
   const double *bathy;      // bed modes [mode][Kp] (shallow water) or null
   const double *vtx;        // element vertices (rows of Kp): positions for a velocity field
   double *T;                // traces of out (TR)
+  const double *M;          // fused limiter: the means of out (k_means), rows of Kp
+  const int *nbr;           // fused limiter: neighbours across faces 0..2, rows of Kp
   double ca, cb, cc;
   int K, Kp, check;
 };
@@ -389,6 +429,49 @@ __global__ void __launch_bounds__(kMaxBlock) k_element(const __grid_constant__ T
                                                        const __grid_constant__ ElemArgs a) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e < a.K) element_body<Eq, P, TR>(tab, q, a, e);
+}
+
+// ---------------------------------------------------------------------------
+// The cell means of a stage's output before its element stage runs, so that
+// the element stage can apply the limiter (which needs the new means of the
+// three neighbours) in its own epilogue.  Basis function 0 is constant and
+// has no gradient, so the mean's right-hand side is the surface term alone:
+// phi_0's edge value times the sum of the element's side fluxes (-F on a
+// left face, +F on a right face), from the per-side sums Fs of the face
+// kernel.  M = ca * un_0 + cb * us_0 + cc * dt / J * that, with the element
+// epilogue's roundings; the element stage writes these M as the output's
+// mode 0, so the limiter's neighbour bounds see exactly the stored means.
+template <class Eq, int P>
+__global__ void __launch_bounds__(kMaxBlock) k_means(const __grid_constant__ Tab<P> tab,
+                                                     const __grid_constant__ ElemArgs a,
+                                                     const double *__restrict__ Fs,
+                                                     double *__restrict__ M) {
+  constexpr int N = Eq::N, NP = Tab<P>::NP;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= a.K) return;
+  const size_t Kp = a.Kp;
+  double sum[N];
+#pragma unroll
+  for (int n = 0; n < N; n++) sum[n] = 0.0;
+#pragma unroll
+  for (int f = 0; f < 3; f++) {
+    const int sd = a.esd[f * Kp + e];
+    double F[N];
+    load_vars<N>(Fs + (size_t)(sd >> 1) * N, F);
+    // the sign as a bit flip (exactly -F), off the FP64 pipe
+    const long long sg = (sd & 1) ? 0ll : (long long)0x8000000000000000ull;
+#pragma unroll
+    for (int n = 0; n < N; n++) sum[n] += __longlong_as_double(sg ^ __double_as_longlong(F[n]));
+  }
+  const double sc = a.cc * *a.dtp * a.geo[4 * Kp + e];
+  const double e0 = tab.E[0][0][0];
+#pragma unroll
+  for (int n = 0; n < N; n++) {
+    const size_t o = (size_t)(n * NP) * Kp + e;
+    double v = fma(sc, sum[n] * e0, a.cb * a.us[o]);
+    if (a.ca != 0.0) v = fma(a.ca, a.un[o], v);
+    M[(size_t)n * Kp + e] = v;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -754,6 +837,8 @@ __device__ __forceinline__ ElemArgs batch_elem_args(const BatchProb &pr, int sta
   a.bathy = pr.bathy;
   a.vtx = pr.vtx;
   a.T = pr.T;
+  a.M = nullptr;
+  a.nbr = pr.nbr;
   a.ca = stage == 0 ? 0.0 : stage == 1 ? 0.75 : 1.0 / 3.0;
   a.cb = stage == 0 ? 1.0 : stage == 1 ? 0.25 : 2.0 / 3.0;
   a.cc = stage == 0 ? 1.0 : stage == 1 ? 0.25 : 2.0 / 3.0;
@@ -795,6 +880,7 @@ __global__ void __launch_bounds__(kMaxBlock)
   a.bxy = pr.bxy;
   a.vtx = pr.vtx;
   a.Fh = pr.Fh;
+  a.Fs = nullptr;
   a.tptr = &pr.ds->t;
   a.dtp = &pr.ds->dt;
   a.tcoef = tcoef;
@@ -888,6 +974,8 @@ struct Launch {
     a.bathy = c.m.bathy;
     a.vtx = c.m.vtx;
     a.T = T;
+    a.M = c.M;
+    a.nbr = c.m.nbr;
     a.ca = ca;
     a.cb = cb;
     a.cc = cc;
@@ -902,7 +990,8 @@ struct Launch {
     DG_DISPATCH_P((k_trace<Eq, P><<<nblk(c.m.K, c.blk), c.blk, 0, c.st>>>(tab<P>(c), *c.q, u,
                                                                           c.T, c.m.K, c.m.Kp)));
   }
-  static void face(const Ctx &c, const double *t, double tcoef) {
+  template <bool FS>
+  static void face_args(const Ctx &c, const double *t, double tcoef, double *Fs) {
     if (!c.m.S) return;
     FaceArgs a;
     a.T = c.T;
@@ -911,13 +1000,31 @@ struct Launch {
     a.bxy = c.m.bxy;
     a.vtx = c.m.vtx;
     a.Fh = c.Fh;
+    a.Fs = Fs;
     a.tptr = t;
     a.dtp = &c.ds->dt;
     a.tcoef = tcoef;
     a.S = c.m.S;
     a.Sb = c.m.Sb;
     a.Kp = c.m.Kp;
-    DG_DISPATCH_P((k_face<Eq, P><<<nblk(c.m.S, c.blk), c.blk, 0, c.st>>>(tab<P>(c), *c.q, a)));
+    DG_DISPATCH_P((k_face<Eq, P, FS><<<nblk(c.m.S, c.blk), c.blk, 0, c.st>>>(tab<P>(c), *c.q,
+                                                                             a)));
+  }
+  static void face(const Ctx &c, const double *t, double tcoef) {
+    face_args<false>(c, t, tcoef, nullptr);
+  }
+  // face() that also leaves the per-side flux sums in c.Fs (instantiated only
+  // where an equation's fused-limiter stage uses it)
+  static void face_fs(const Ctx &c, const double *t, double tcoef) {
+    face_args<true>(c, t, tcoef, c.Fs);
+  }
+  // the means of a stage's output into c.M (k_means)
+  static void means(const Ctx &c, double *us, const double *un, double ca, double cb, double cc,
+                    const double *dtp) {
+    if (!c.m.K) return;
+    const ElemArgs a = eargs(c, us, un, nullptr, ca, cb, cc, dtp, nullptr, 0);
+    DG_DISPATCH_P((k_means<Eq, P><<<nblk(c.m.K, c.blk), c.blk, 0, c.st>>>(tab<P>(c), a, c.Fs,
+                                                                          c.M)));
   }
   static void element(const Ctx &c, double *us, const double *un, double *out, double ca,
                       double cb, double cc, const double *dtp) {
@@ -964,8 +1071,8 @@ struct Launch {
 #undef DG_DISPATCH_P
 
   static const Ops &ops() {
-    static const Ops o = {trace, face, element, limit, lambda, init, l2err, element_tr,
-                          limit_tr, vertex};
+    static const Ops o = {trace,  face,       element,  limit,  lambda,  init,    l2err,
+                          element_tr, limit_tr, vertex, nullptr, nullptr, nullptr};
     return o;
   }
 

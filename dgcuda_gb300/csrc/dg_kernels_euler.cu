@@ -1,18 +1,22 @@
 // dg_kernels_euler.cu -- kernel instances for the Euler module, p = 0..5;
-// the fused element stage runs on the tensor cores (dg_ozaki.cuh) for
-// p = 1..4 when the solver has built its tables (Ctx::oz).
-#include "dg_ozaki.cuh"
+// the fused element stage runs on the tensor cores (dg_ozaki.cuh, one
+// translation unit per order: dg_ozaki_euler_p*.cu) for p = 1..4 when the
+// solver has built its tables (Ctx::oz), with the limiter in its epilogue
+// when the limiter is on (element_lim).
+#include "dg_ozaki_euler.cuh"
 
 namespace dg {
 namespace {
 
 using L = Launch<Euler>;
 
-template <int P>
-void oz_element(const Ctx &c, const ElemArgs &a) {
-  const unsigned blocks = (unsigned)((c.m.K + oz::kOzElems - 1) / oz::kOzElems);
-  oz::k_element_oz<Euler, P><<<blocks, oz::kOzThreads, oz::oz_smem_bytes<Euler, P>(), c.st>>>(
-      L::tab<P>(c), *c.q, a, static_cast<const oz::Tabs *>(c.oz));
+void oz_element(const Ctx &c, const ElemArgs &a, bool lim) {
+  switch (c.p) {
+    case 1: oz::euler_element<1>(c, a, lim); break;
+    case 2: oz::euler_element<2>(c, a, lim); break;
+    case 3: oz::euler_element<3>(c, a, lim); break;
+    case 4: oz::euler_element<4>(c, a, lim); break;
+  }
 }
 
 void element_tr(const Ctx &c, double *us, const double *un, double *out, double ca, double cb,
@@ -22,13 +26,15 @@ void element_tr(const Ctx &c, double *us, const double *un, double *out, double 
     return;
   }
   if (!c.m.K) return;
-  const ElemArgs a = L::eargs(c, us, un, out, ca, cb, cc, dtp, c.T, check);
-  switch (c.p) {
-    case 1: oz_element<1>(c, a); break;
-    case 2: oz_element<2>(c, a); break;
-    case 3: oz_element<3>(c, a); break;
-    case 4: oz_element<4>(c, a); break;
-  }
+  oz_element(c, L::eargs(c, us, un, out, ca, cb, cc, dtp, c.T, check), false);
+}
+
+// the element stage with the limiter in its epilogue (tensor path only; M
+// holds the output's means from k_means)
+void element_lim(const Ctx &c, double *us, const double *un, double *out, double ca, double cb,
+                 double cc, const double *dtp) {
+  if (!c.m.K) return;
+  oz_element(c, L::eargs(c, us, un, out, ca, cb, cc, dtp, c.T, 0), true);
 }
 
 void trace(const Ctx &c, double *u) {
@@ -37,13 +43,11 @@ void trace(const Ctx &c, double *u) {
     return;
   }
   if (!c.m.K) return;
-  const unsigned blocks = (unsigned)((c.m.K + oz::kOzElems - 1) / oz::kOzElems);
-  const oz::Tabs *t = static_cast<const oz::Tabs *>(c.oz);
   switch (c.p) {
-    case 1: oz::k_trace_oz<Euler, 1><<<blocks, oz::kOzThreads, 0, c.st>>>(L::tab<1>(c), *c.q, u, c.T, c.m.K, c.m.Kp, t); break;
-    case 2: oz::k_trace_oz<Euler, 2><<<blocks, oz::kOzThreads, 0, c.st>>>(L::tab<2>(c), *c.q, u, c.T, c.m.K, c.m.Kp, t); break;
-    case 3: oz::k_trace_oz<Euler, 3><<<blocks, oz::kOzThreads, 0, c.st>>>(L::tab<3>(c), *c.q, u, c.T, c.m.K, c.m.Kp, t); break;
-    case 4: oz::k_trace_oz<Euler, 4><<<blocks, oz::kOzThreads, 0, c.st>>>(L::tab<4>(c), *c.q, u, c.T, c.m.K, c.m.Kp, t); break;
+    case 1: oz::euler_trace<1>(c, u); break;
+    case 2: oz::euler_trace<2>(c, u); break;
+    case 3: oz::euler_trace<3>(c, u); break;
+    case 4: oz::euler_trace<4>(c, u); break;
   }
 }
 
@@ -51,14 +55,10 @@ Ops make_ops() {
   Ops o = L::ops();
   o.element_tr = element_tr;
   o.trace = trace;
+  o.face_fs = L::face_fs;
+  o.means = L::means;
+  o.element_lim = element_lim;
   return o;
-}
-
-template <int P>
-cudaError_t oz_attr() {
-  return cudaFuncSetAttribute(oz::k_element_oz<Euler, P>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)oz::oz_smem_bytes<Euler, P>());
 }
 
 }  // namespace
@@ -69,14 +69,14 @@ const Ops &ops_euler() {
 }
 const BatchOps &batch_ops_euler() { return Launch<Euler>::batch_ops(); }
 
-// allows the tensor-core element kernel of order p its shared memory (once
-// per device, before any capture)
+// allows the tensor-core element kernels of order p their shared memory
+// (once per device, before any capture)
 cudaError_t oz_prepare_euler(int p) {
   switch (p) {
-    case 1: return oz_attr<1>();
-    case 2: return oz_attr<2>();
-    case 3: return oz_attr<3>();
-    case 4: return oz_attr<4>();
+    case 1: return oz::euler_prepare<1>();
+    case 2: return oz::euler_prepare<2>();
+    case 3: return oz::euler_prepare<3>();
+    case 4: return oz::euler_prepare<4>();
     default: return cudaErrorInvalidValue;
   }
 }

@@ -65,6 +65,8 @@ struct Ctx {
   const void *tab = nullptr;      // host Tab<p> image
   double *T = nullptr;            // traces [elem][face][j][var]
   double *Fh = nullptr;           // face fluxes [side][j][var], scaled by len/2 * w_j
+  double *Fs = nullptr;           // per-side sums of Fh over the edge points [side][var]
+  double *M = nullptr;            // means of the stage output [var][Kp] (fused limiter)
   DevScalars *ds = nullptr;       // device scalars
   const void *oz = nullptr;       // tensor-core tables of order p (null: FP64 contractions)
 };
@@ -139,6 +141,16 @@ struct Ops {
   void (*limit_tr)(const Ctx &, double *u);
   // values of variable var at the three vertices, rows of Kp: out[v][elem]
   void (*vertex)(const Ctx &, const double *u, int var, int mode, double t, double *out);
+  // a stage with the limiter in the element stage's epilogue (null where an
+  // equation has none): face() that also leaves the per-side flux sums in
+  // Fs; the means of the stage output into M (k_means); element_tr() that
+  // limits its output (Barth-Jespersen with the neighbours' means from M),
+  // applies the positivity rule to the limited traces and writes both
+  void (*face_fs)(const Ctx &, const double *t, double tcoef);
+  void (*means)(const Ctx &, double *us, const double *un, double ca, double cb, double cc,
+                const double *dtp);
+  void (*element_lim)(const Ctx &, double *us, const double *un, double *out, double ca,
+                      double cb, double cc, const double *dtp);
 };
 
 const Ops &ops_advection();

@@ -273,6 +273,9 @@ struct OzShape {
   // new traces live in the same slots (gh_slot)
   static constexpr int GH = 2 * PQ * 2 * N;
   static_assert(PF <= 2 * PQ, "the traces of a variable fit its g, h slots");
+  // a variable's g/h position PF, unused by its traces: where the fused
+  // limiter keeps modes 1 and 2 of the unlimited output (p >= 2)
+  static constexpr bool kStash = PF < 2 * PQ;
   static constexpr size_t kSmem = (size_t)4 * GH * 32 * sizeof(double);
 };
 
@@ -303,9 +306,129 @@ __device__ __forceinline__ void split_rows(const double (&x)[2][4], int (&m)[2],
   }
 }
 
+// The limiter in the element stage's epilogue (limit_tr_body's rules), after
+// the stage has written its unlimited output and staged its new traces in gh.
+// Lane t of a quad limits variable t of the quad's two elements, so alpha and
+// the bounds are found once per element and variable (N <= 4):
+//  * each lane takes the extremes of the staged traces at its own positions,
+//    for every variable, as order keys on the integer pipe; a reduce-scatter
+//    over the quad leaves lane t the extremes of variable t;
+//  * lane t forms the bounds from the means of the element and its three
+//    neighbours (a.M, a.nbr) and alpha;
+//  * where alpha < 1 it scales modes 1 and 2 (from the stash slot, else from
+//    the output) in the output, drops the higher modes and rebuilds all of
+//    variable t's staged traces (every position, in the four lanes'
+//    columns): the mean where alpha = 0, else a0 + c1 E_1 + c2 E_2, with
+//    compile-time table indices.
+template <class Eq, int P>
+__device__ __forceinline__ void limit_epilogue(const Tab<P> &tab, const ElemArgs &a, double *gh,
+                                               int lane, const int (&ec)[2], const int (&el)[2],
+                                               const bool (&live)[2]) {
+  using S = OzShape<Eq, P>;
+  constexpr int N = S::N, NP = S::NP, N1 = S::N1, NF = S::NF, PF = S::PF;
+  static_assert(N <= 4, "one variable per lane of a quad");
+  const int t = lane & 3, q0 = lane & ~3;
+  const size_t Kp = a.Kp;
+  const double phi0 = tab.B[0][0], e0 = tab.E[0][0][0];
+  // ---- extremes: per lane and variable, then reduce-scatter over the quad
+  long long kx[2][4], kn[2][4];
+#pragma unroll
+  for (int e = 0; e < 2; e++)
+#pragma unroll
+    for (int n = 0; n < 4; n++) {
+      kx[e][n] = (long long)0x8000000000000000ull;
+      kn[e][n] = 0x7FFFFFFFFFFFFFFFll;
+      if (n >= N) continue;
+#pragma unroll
+      for (int p = 0; p < PF; p++)
+        if (p * 4 + t < NF) {
+          const long long k = order_key(gh[gh_slot<N>(n, p >> 1, e, p & 1) + lane]);
+          kx[e][n] = max(kx[e][n], k);
+          kn[e][n] = min(kn[e][n], k);
+        }
+    }
+  // step 1 (partner t ^ 1): keep the variables whose bit 0 is t's, send the
+  // others; step 2 (partner t ^ 2): the same on bit 1 -- lane t ends with t
+  const bool b0 = t & 1, b1 = t & 2;
+  long long hx[2][2], hn[2][2];
+#pragma unroll
+  for (int e = 0; e < 2; e++)
+#pragma unroll
+    for (int h = 0; h < 2; h++) {  // variables 2h + {0, 1}
+      const long long sx = b0 ? kx[e][2 * h] : kx[e][2 * h + 1];
+      const long long sn = b0 ? kn[e][2 * h] : kn[e][2 * h + 1];
+      const long long rx = __shfl_xor_sync(0xffffffffu, sx, 1);
+      const long long rn = __shfl_xor_sync(0xffffffffu, sn, 1);
+      hx[e][h] = max(b0 ? kx[e][2 * h + 1] : kx[e][2 * h], rx);
+      hn[e][h] = min(b0 ? kn[e][2 * h + 1] : kn[e][2 * h], rn);
+    }
+  long long mx[2], mn[2];
+#pragma unroll
+  for (int e = 0; e < 2; e++) {
+    const long long sx = b1 ? hx[e][0] : hx[e][1];
+    const long long sn = b1 ? hn[e][0] : hn[e][1];
+    const long long rx = __shfl_xor_sync(0xffffffffu, sx, 2);
+    const long long rn = __shfl_xor_sync(0xffffffffu, sn, 2);
+    mx[e] = max(b1 ? hx[e][1] : hx[e][0], rx);
+    mn[e] = min(b1 ? hn[e][1] : hn[e][0], rn);
+  }
+  if (t >= N) return;  // (no lane is idle at N = 4)
+  const int n = t;
+  const double *Mn = a.M + (size_t)n * Kp;
+  double *outn = a.out + (size_t)(n * NP) * Kp;
+#pragma unroll
+  for (int e = 0; e < 2; e++) {
+    const double c0 = Mn[ec[e]];
+    const int nb0 = a.nbr[ec[e]], nb1 = a.nbr[Kp + ec[e]], nb2 = a.nbr[2 * Kp + ec[e]];
+    // products reused as addends are rounded explicitly, as in limit_tr_body
+    const double Uc = __dmul_rn(c0, phi0);
+    double Umin, Umax;
+    mean_bounds(c0, Mn[nb0], Mn[nb1], Mn[nb2], phi0, Umin, Umax);
+    const double up = fmax(0.0, from_order_key(mx[e]) - Uc);
+    const double dn = fmax(0.0, Uc - from_order_key(mn[e]));
+    double al = 1.0;
+    const double lo = Uc - Umin, hi = Umax - Uc;
+    if (up > lo) al = fmin(al, __double_as_longlong(lo) ? lo / up : 0.0);
+    if (dn > hi) al = fmin(al, __double_as_longlong(hi) ? hi / dn : 0.0);
+    if (al < 0.0) al = 0.0;
+    if (!(al < 1.0) || !live[e]) continue;
+    double c1, c2;
+    if constexpr (S::kStash) {
+      c1 = gh[gh_slot<N>(n, PF >> 1, e, PF & 1) + (q0 | 1)] * al;
+      c2 = gh[gh_slot<N>(n, PF >> 1, e, PF & 1) + (q0 | 2)] * al;
+    } else {
+      c1 = outn[(size_t)1 * Kp + el[e]] * al;
+      c2 = outn[(size_t)2 * Kp + el[e]] * al;
+    }
+    outn[(size_t)1 * Kp + el[e]] = c1;
+    outn[(size_t)2 * Kp + el[e]] = c2;
+#pragma unroll
+    for (int i = 3; i < NP; i++) outn[(size_t)i * Kp + el[e]] = 0.0;
+    // basis function 0 is constant: c0 phi_0 is one product for every point
+    const double a0 = c0 * e0;
+    const bool flat = al == 0.0 && a0 != 0.0;
+#pragma unroll
+    for (int idx = 0; idx < NF; idx++) {
+      const int f = idx / N1, j = idx % N1, pp = idx >> 2, tt = idx & 3;
+      double v = a0;
+      if (!flat) {
+        v = fma(c1, tab.E[f][j][1], v);
+        v = fma(c2, tab.E[f][j][2], v);
+      }
+      gh[gh_slot<N>(n, pp >> 1, e, pp & 1) + (q0 | tt)] = v;
+    }
+  }
+}
+
 // 4 blocks per SM (128 registers) up to p = 3, where the extra warps hide
 // more latency than the spills cost; at p = 4 the shared memory holds 3
-template <class Eq, int P>
+// LIM: the limiter in the epilogue (the fused SSP-RK3 stage with the limiter
+// on): the output's means are a.M (k_means, from the same stage's side-flux
+// sums); each variable's new traces give its edge extremes, the means of the
+// element and its three neighbours (a.nbr) give the bounds, and the limited
+// modes and traces -- limit_tr_body's rules -- are what is written; the
+// positivity rule is then applied to the limited traces (limit_epilogue).
+template <class Eq, int P, bool LIM = false>
 __global__ void __launch_bounds__(kOzThreads, P <= 3 ? 4 : 3) k_element_oz(const __grid_constant__ Tab<P> tab,
                                                            const __grid_constant__ EqP q,
                                                            const __grid_constant__ ElemArgs a,
@@ -336,6 +459,13 @@ __global__ void __launch_bounds__(kOzThreads, P <= 3 ? 4 : 3) k_element_oz(const
     for (int r = 0; r < 5; r++) prefetch_l1(a.geo + (size_t)r * Kp + ec[e]);
 #pragma unroll
     for (int f = 0; f < 3; f++) prefetch_l1(a.esd + (size_t)f * Kp + ec[e]);
+  }
+  // LIM: the limiter's neighbour indices and this lane's variable's mean
+#pragma unroll
+  for (int e = 0; e < 2 && LIM; e++) {
+#pragma unroll
+    for (int f = 0; f < 3; f++) prefetch_l1(a.nbr + (size_t)f * Kp + ec[e]);
+    if (t < N) prefetch_l1(a.M + (size_t)t * Kp + ec[e]);
   }
   // ---- area-point values of every variable -> ub ----
 #pragma unroll 1
@@ -601,6 +731,9 @@ __global__ void __launch_bounds__(kOzThreads, P <= 3 ? 4 : 3) k_element_oz(const
           const double cin = (badv[e] && idx > 0) ? 0.0 : us[o];
           double v = fma(sc[e], R[p < PM ? p : 0][e], a.cb * cin);
           if (a.ca != 0.0) v = fma(a.ca, a.un[o], v);
+          // LIM: mode 0 is the mean k_means stored, which the neighbours'
+          // limiters read (the same value up to the rounding of its sum)
+          if (LIM && idx == 0) v = a.M[(size_t)n * Kp + ec[e]];
           if (live[e]) {
             a.out[o] = v;
             if (badv[e] && idx > 0 && a.us != a.out) a.us[o] = 0.0;
@@ -608,6 +741,13 @@ __global__ void __launch_bounds__(kOzThreads, P <= 3 ? 4 : 3) k_element_oz(const
           cnew[e][p] = v;
         }
       }
+    // LIM: modes 1 and 2 (position 0 of lanes t = 1, 2) for the limiter,
+    // in a g/h slot of this variable that its traces leave free
+    if constexpr (LIM && S::kStash) {
+#pragma unroll
+      for (int e = 0; e < 2; e++)
+        gh[gh_slot<N>(n, PF >> 1, e, PF & 1) + lane] = cnew[e][0];
+    }
     // next-stage edge traces
     int m[2];
     long long Y[2][4];
@@ -620,6 +760,13 @@ __global__ void __launch_bounds__(kOzThreads, P <= 3 ? 4 : 3) k_element_oz(const
       for (int e = 0; e < 2; e++)
         gh[gh_slot<N>(n, p >> 1, e, p & 1) + lane] =
             recombine(acc, p >> 1, 2 * e + (p & 1), m[e], ozt->colexp[kTrace][slot_of(p, t)]);
+  }
+
+  // the limiter, one variable per lane of each quad, after the loop above
+  // (its inputs were staged by the other lanes of the quad)
+  if constexpr (LIM) {
+    __syncwarp();
+    limit_epilogue<Eq, P>(tab, a, gh, lane, ec, el, live);
   }
 
   // lane t = 0 wrote each element's mode 0 to out; the flatten below reads it
@@ -638,7 +785,7 @@ __global__ void __launch_bounds__(kOzThreads, P <= 3 ? 4 : 3) k_element_oz(const
     }
 #pragma unroll
   for (int e = 0; e < 2; e++) {
-    int b = badt[e] && a.check;
+    int b = badt[e] && (LIM || a.check);
     b |= __shfl_xor_sync(0xffffffffu, b, 1);
     b |= __shfl_xor_sync(0xffffffffu, b, 2);
     badt[e] = b != 0;

@@ -27,8 +27,8 @@ struct ProfEvent {
   int kind;
   cudaEvent_t a, b;
 };
-const char *kKindName[] = {"trace", "face", "element", "limit", "cfl", "rk"};
-constexpr int kKinds = 6;
+const char *kKindName[] = {"trace", "face", "element", "limit", "cfl", "rk", "means"};
+constexpr int kKinds = 7;
 
 }  // namespace
 
@@ -46,6 +46,7 @@ struct dg_solver {
   const dg::Ops *ops = nullptr;
   double *U = nullptr, *W = nullptr, *k[4] = {nullptr, nullptr, nullptr, nullptr};
   double *ubuf = nullptr, *partial = nullptr, *T = nullptr, *Fh = nullptr, *vbuf = nullptr;
+  double *Fs = nullptr, *M = nullptr;  // side-flux sums and output means (fused limiter)
   double *bathy = nullptr;        // bed modes (shallow water), internal order
   double *lin_tv = nullptr, *lin_f0 = nullptr, *lin_f1 = nullptr;  // adjoint work
   bool has_inout_bc = false;      // a side with an inflow or outflow code
@@ -157,7 +158,7 @@ void collect_profile(dg_solver *s) {
   s->pending.clear();
 }
 
-enum { K_TRACE = 0, K_FACE = 1, K_ELEMENT = 2, K_LIMIT = 3, K_CFL = 4, K_RK = 5 };
+enum { K_TRACE = 0, K_FACE = 1, K_ELEMENT = 2, K_LIMIT = 3, K_CFL = 4, K_RK = 5, K_MEANS = 6 };
 
 // one RK stage of the DG operator: out = ca*un + cb*us + cc*dt*L(us).
 // With the tensor-core contractions on, the element stage is the one the
@@ -179,10 +180,20 @@ void limit(dg_solver *s, double *u) {
 }
 
 // a stage whose input traces are already in T (left by the previous stage);
-// it leaves the traces of `out` -- limited when the limiter is on -- in T
+// it leaves the traces of `out` -- limited when the limiter is on -- in T.
+// With the limiter on and the tensor-core element stage, the limiter runs in
+// that stage's epilogue: the face kernel also sums each side's fluxes, and
+// k_means turns the sums into the output's cell means, which the element
+// stage needs for its neighbours' bounds; no separate limiter pass.
 void fused_stage(dg_solver *s, double *us, const double *un, double *out, double ca, double cb,
                  double cc, double tcoef, const double *dtp) {
   const bool lim = s->prm.limiter && s->np >= 3;
+  if (lim && s->ctx.oz && s->ops->element_lim && s->ctx.M) {
+    run(s, K_FACE, [&] { s->ops->face_fs(s->ctx, &s->ds->t, tcoef); });
+    run(s, K_MEANS, [&] { s->ops->means(s->ctx, us, un, ca, cb, cc, dtp); });
+    run(s, K_ELEMENT, [&] { s->ops->element_lim(s->ctx, us, un, out, ca, cb, cc, dtp); });
+    return;
+  }
   run(s, K_FACE, [&] { s->ops->face(s->ctx, &s->ds->t, tcoef); });
   run(s, K_ELEMENT,
       [&] { s->ops->element_tr(s->ctx, us, un, out, ca, cb, cc, dtp, lim ? 0 : 1); });
@@ -600,6 +611,10 @@ extern "C" dg_status dg_solver_create(const dg_mesh *mesh, dg_equation eq, int p
   if ((st = dalloc(s, &s->ubuf, nuser)) != DG_OK) return bail(st);
   if ((st = dalloc(s, &s->T, (size_t)K * 3 * n1 * s->N)) != DG_OK) return bail(st);
   if ((st = dalloc(s, &s->Fh, (size_t)S * n1 * s->N)) != DG_OK) return bail(st);
+  if (s->ops->element_lim) {
+    if ((st = dalloc(s, &s->Fs, (size_t)S * s->N)) != DG_OK) return bail(st);
+    if ((st = dalloc(s, &s->M, (size_t)s->N * Kp)) != DG_OK) return bail(st);
+  }
   if ((st = dalloc(s, &s->partial, (size_t)s->N * ((K + 127) / 128 + 1))) != DG_OK) return bail(st);
   if ((st = dalloc(s, &s->ds, 1)) != DG_OK) return bail(st);
   if ((st = dalloc(s, &s->vbuf, (size_t)6 * Kp)) != DG_OK) return bail(st);
@@ -625,6 +640,8 @@ extern "C" dg_status dg_solver_create(const dg_mesh *mesh, dg_equation eq, int p
   c.tab = s->tabimg.data();
   c.T = s->T;
   c.Fh = s->Fh;
+  c.Fs = s->Fs;
+  c.M = s->M;
   c.ds = s->ds;
   dg_status ozs = oz_refresh(s);
   if (ozs != DG_OK) return bail(ozs);

@@ -316,7 +316,8 @@ void dg_adjoint_destroy(dg_adjoint *a);
  * solver stream).  When enabled, dg_step launches kernels directly instead
  * of replaying a CUDA graph. */
 dg_status dg_profile_enable(dg_solver *s, int on);
-/* names: "trace", "face", "element", "limit", "cfl"; fills launches and the
+/* names: "trace", "face", "element", "limit", "cfl", "rk", "means" (the
+ * fused limiter's cell means); fills launches and the
  * summed milliseconds since the last reset */
 dg_status dg_profile_get(dg_solver *s, const char *kernel, long long *launches, double *ms);
 dg_status dg_profile_reset(dg_solver *s);

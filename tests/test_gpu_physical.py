@@ -50,6 +50,12 @@ def test_filter_settles_ordinary_states(dglib):
     assert exact.all() and fast.all()
     fast, exact = dg.probe_physical(states(rho, u, v, -p))
     assert not exact.any() and not fast.any()
+    # gas at rest along one axis or both (an exact zero momentum component,
+    # as in the uniform quadrants of a Riemann problem) is settled too
+    zero = np.zeros(n)
+    for uu, vv in ((zero, v), (u, zero), (zero, zero)):
+        fast, exact = dg.probe_physical(states(rho, uu, vv, p))
+        assert exact.all() and fast.all()
 
 
 def test_sound_speed_sqrt_within_one_ulp(dglib):
