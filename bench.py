@@ -203,7 +203,7 @@ def ensemble_bench(device, nprob, steps, warmup, seed=4000):
                     "captured dg_step in sequence"}
 
 
-def adjoint_bench(device, n=256, steps=2000, ckpt=50, nrec=64, nsamp=20, seed=5):
+def adjoint_bench(device, n=256, steps=2000, ckpt=50, nrec=64, nsamp=20, seed=5, fd_dirs=16):
     """Config 5: discrete adjoint of shallow water on n x n jittered squares
     (2 n^2 triangles), p=2, Gaussian hump over the sine bed, reflecting
     walls, SSP-RK3 at a fixed dt, `steps` steps with checkpoints every
@@ -213,11 +213,16 @@ def adjoint_bench(device, n=256, steps=2000, ckpt=50, nrec=64, nsamp=20, seed=5)
     0.02 N(0,1) sin(2 pi kx x) sin(2 pi ky y), projected on the basis.  (White
     noise of 0.02 N(0,1) in every element mode gives bed slopes of order 25
     at this resolution; without well-balancing for beds that jump between
-    elements the observation run then loses its depth and fails.)  Times (CUDA events on the solver stream): the plain forward
-    (graph-captured dg_step), the checkpointing forward and the backward
-    sweep (segment recompute + adjoint stages).  Accuracy: the gradient
-    along one seeded direction against central differences, and the
-    tangent-linear / adjoint dot product."""
+    elements the observation run then loses its depth and fails.)
+
+    Times (CUDA events on the solver stream): the plain forward
+    (graph-captured dg_step), then the gradient two ways -- the forward run
+    keeping every stage state in device memory (3 x steps states; the
+    reverse sweep recomputes nothing) and the forward run keeping the
+    checkpoints only (the reverse sweep recomputes each segment) -- each as
+    forward + backward.  Accuracy: the gradient against central differences
+    (step 1e-6) along `fd_dirs` seeded directions of the initial height and
+    the bed modes, and the tangent-linear / adjoint dot product."""
     import torch
     import dgcuda_gb300 as dg
     from dgcuda_gb300.ensemble import WALLS
@@ -255,59 +260,78 @@ def adjoint_bench(device, n=256, steps=2000, ckpt=50, nrec=64, nsamp=20, seed=5)
             s.bathymetry_project("sine", (1.0, kx, ky))
             pert += 0.02 * rng.standard_normal() * s.get_bathymetry()
     s.set_bathymetry(b0 + pert)
-    obs = adj.forward(steps, dt, every, ckpt)
+    obs = adj.forward(steps, dt, every, ckpt)  # also allocates what forward keeps
     # plain forward: the same steps through the captured fused step
     reset()
     s.step(3, dg.SSP_RK3, 0.0)
     reset()
     _, fwd_plain = timed(lambda: s.step(steps, dg.SSP_RK3, 0.0))
-    reset()
-    smp, fwd_ckpt = timed(lambda: adj.forward(steps, dt, every, ckpt))
-    (gu, gb), bwd = timed(lambda: adj.backward(2 * (smp - obs)))
-    # accuracy along one seeded direction (initial height + bed modes)
-    dh = rng.standard_normal(c0[0].shape)
-    dbd = rng.standard_normal(b0.shape)
-    dh /= np.linalg.norm(dh)
-    dbd /= np.linalg.norm(dbd)
+    modes = {}
+    for keep in (True, False):
+        adj.set_storage(keep)
+        reset()
+        adj.forward(steps, dt, every, ckpt)  # warm (allocations of this mode)
+        reset()
+        smp, fwd = timed(lambda: adj.forward(steps, dt, every, ckpt))
+        kept = adj.stored
+        (gu, gb), bwd = timed(lambda: adj.backward(2 * (smp - obs)))
+        modes["stored" if keep else "checkpoints"] = {
+            "stage_states_kept": kept, "forward_ms": fwd, "backward_ms": bwd,
+            "adjoint_over_forward": bwd / fwd_plain,
+            "gradient_over_forward": (fwd + bwd) / fwd_plain, "grad": (gu, gb)}
+    gu, gb = modes["stored"]["grad"]
+    gu2, gb2 = modes["checkpoints"].pop("grad")
+    modes["stored"].pop("grad")
+    same = bool(np.array_equal(gu, gu2) and np.array_equal(gb, gb2))
+    # central differences along fd_dirs seeded directions (forward runs that
+    # keep the checkpoints only: they are cheaper and give the same samples)
+    adj.set_storage(False)
 
-    def J(e):
+    def J(e, dh, dbd):
         reset(b0 + e * dbd, c0[0] + e * dh)
         return float(np.sum((adj.forward(steps, dt, every, ckpt) - obs) ** 2))
 
-    def fd_at(e):
-        return (J(e) - J(-e)) / (2 * e)
-
-    eps = 1e-6
-    fd, fd_half = fd_at(eps), fd_at(eps / 2)
-    for _ in range(4):
-        if abs(fd - fd_half) <= 1e-7 * abs(fd_half):
-            break
-        eps /= 2
-        fd, fd_half = fd_half, fd_at(eps / 2)
-    ad = float(np.sum(gu[0] * dh) + np.sum(gb * dbd))
+    eps, errs = 1e-6, []
+    for _ in range(fd_dirs):
+        dh = rng.standard_normal(c0[0].shape)
+        dbd = rng.standard_normal(b0.shape)
+        dh /= np.linalg.norm(dh)
+        dbd /= np.linalg.norm(dbd)
+        fd = (J(eps, dh, dbd) - J(-eps, dh, dbd)) / (2 * eps)
+        ad = float(np.sum(gu[0] * dh) + np.sum(gb * dbd))
+        errs.append(abs(fd - ad) / abs(ad))
+    adj.set_storage(True)
     reset()
     adj.forward(steps, dt, every, ckpt)
-    sbar = rng.standard_normal(smp.shape)
+    sbar = rng.standard_normal(obs.shape)
     du0 = np.zeros(s.shape)
-    du0[0] = dh
+    du0[0] = rng.standard_normal(c0[0].shape)
+    dbd = rng.standard_normal(b0.shape)
     gu2, gb2 = adj.backward(sbar)
     ds = adj.tangent(du0, dbd)
     lhs = float(np.sum(sbar * ds))
     rhs = float(np.sum(gu2 * du0) + np.sum(gb2 * dbd))
     ndof = s.N * s.n_p * s.K
-    finite = bool(np.isfinite(obs).all() and np.isfinite(smp).all() and np.isfinite(gu).all())
+    finite = bool(np.isfinite(obs).all() and np.isfinite(gu).all())
+    st = modes["stored"]
     out = {"finite": finite, "triangles": s.K, "p": 2, "steps": steps, "checkpoint_every": ckpt,
-           "receivers": nrec, "samples": nsamp, "dt": dt,
-           "forward_ms": fwd_plain, "forward_checkpointing_ms": fwd_ckpt, "backward_ms": bwd,
-           "adjoint_over_forward": bwd / fwd_plain,
-           "gradient_over_forward": (fwd_ckpt + bwd) / fwd_plain,
+           "receivers": nrec, "samples": nsamp, "dt": dt, "forward_ms": fwd_plain,
+           "forward_checkpointing_ms": st["forward_ms"], "backward_ms": st["backward_ms"],
+           "adjoint_over_forward": st["adjoint_over_forward"],
+           "gradient_over_forward": st["gradient_over_forward"],
+           "stage_states_kept": st["stage_states_kept"], "modes": modes,
+           "gradients_identical_across_modes": same,
            "forward_dof_stage_per_s": ndof * 3 * steps / (fwd_plain / 1e3),
-           "fd_rel_error": abs(fd - ad) / abs(ad), "fd_step": eps,
+           "fd_directions": fd_dirs, "fd_step": eps,
+           "fd_rel_error_max": max(errs) if errs else None,
+           "fd_rel_error_median": float(np.median(errs)) if errs else None,
            "dot_product_rel_error": abs(lhs - rhs) / max(abs(lhs), abs(rhs)),
+           "stage_state_bytes": 3 * steps * ndof * 8,
            "checkpoint_bytes": ((steps + ckpt - 1) // ckpt + 3 * ckpt) * ndof * 8,
-           "note": "CUDA events on the solver stream; adjoint_over_forward = backward sweep "
-                   "(segment recompute + adjoint stages) / plain forward; "
-                   "gradient_over_forward adds the checkpointing forward"}
+           "note": "CUDA events on the solver stream; gradient_over_forward = (forward that "
+                   "keeps what the reverse sweep needs + reverse sweep) / plain forward; "
+                   "'stored' keeps every stage state in HBM, 'checkpoints' keeps the "
+                   "checkpoints and recomputes each segment"}
     adj.close()
     s.close()
     return out
@@ -367,6 +391,8 @@ def main():
     ap.add_argument("--ensemble-steps", type=int, default=5)
     ap.add_argument("--adjoint-steps", type=int, default=2000,
                     help="steps of the shallow-water adjoint run (0: skip)")
+    ap.add_argument("--adjoint-fd-dirs", type=int, default=16,
+                    help="finite-difference directions of the adjoint gradient check")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -507,7 +533,7 @@ def main():
 
     adjoint = None
     if args.adjoint_steps > 0:
-        adjoint = adjoint_bench(local, steps=args.adjoint_steps)
+        adjoint = adjoint_bench(local, steps=args.adjoint_steps, fd_dirs=args.adjoint_fd_dirs)
 
     cb = None
     if rank == 0 and not args.no_cpu:

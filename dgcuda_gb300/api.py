@@ -136,6 +136,8 @@ def _declare(L):
         "dg_adjoint_backward": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
         "dg_adjoint_tangent": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
         "dg_adjoint_destroy": (None, [C.c_void_p]),
+        "dg_adjoint_set_storage": (C.c_int, [C.c_void_p, C.c_int]),
+        "dg_adjoint_stored": (C.c_int, [C.c_void_p, _ip]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(L, name, None)
@@ -200,6 +202,19 @@ class Adjoint:
         out = np.empty((max(self.nsamp, 1), max(self.nrec, 1)))
         _check(self._L.dg_adjoint_forward(self._h, nsteps, dt, every, ckpt, t0, _dptr(out)))
         return out[:self.nsamp, :self.nrec]
+
+    def set_storage(self, keep_stages):
+        """True: keep every step's stage states in device memory when they
+        fit (the default; the reverse sweep then recomputes nothing); False:
+        the checkpoints only."""
+        _check(self._L.dg_adjoint_set_storage(self._h, int(bool(keep_stages))))
+
+    @property
+    def stored(self):
+        """True when the last forward run kept every stage state."""
+        v = np.zeros(1, dtype=np.int32)
+        _check(self._L.dg_adjoint_stored(self._h, _iptr(v)))
+        return bool(v[0])
 
     def backward(self, sbar):
         s = self.solver

@@ -1494,6 +1494,14 @@ struct dg_adjoint {
   double *rec_phi = nullptr, *samples = nullptr, *sbar = nullptr;
   std::vector<double *> cks;                  // checkpoints u^{k ckpt}
   std::vector<double *> seg;                  // 3 ckpt states of a segment: u^n, u1, u2
+  // every step's u^n, u1, u2 ([3 nsteps][ndof_p]) when they fit in device
+  // memory (keep != 0): the reverse sweep then recomputes nothing
+  int keep = 1;
+  bool stored = false;
+  double *store = nullptr;
+  size_t store_n = 0;
+  double *ufinal = nullptr;                   // the forward run's final state
+  double t_end = 0;                           // and its time
   double *ub = nullptr, *ub1 = nullptr, *ub2 = nullptr, *acc = nullptr, *bbar = nullptr;
   double *du = nullptr, *dw = nullptr, *dbi = nullptr;
   std::vector<void *> mem;
@@ -1605,6 +1613,27 @@ extern "C" void dg_adjoint_destroy(dg_adjoint *a) {
   delete a;
 }
 
+extern "C" dg_status dg_adjoint_set_storage(dg_adjoint *a, int keep_stages) {
+  if (!a || keep_stages < 0 || keep_stages > 1) return fail(DG_BAD_ARG, "bad arguments");
+  a->keep = keep_stages;
+  if (!keep_stages && a->store) {
+    cudaSetDevice(a->s->device);
+    cudaStreamSynchronize(a->s->st);
+    cudaFree(a->store);
+    a->mem.erase(std::find(a->mem.begin(), a->mem.end(), (void *)a->store));
+    a->store = nullptr;
+    a->store_n = 0;
+    a->stored = false;
+  }
+  return DG_OK;
+}
+
+extern "C" dg_status dg_adjoint_stored(const dg_adjoint *a, int *kept) {
+  if (!a || !kept) return fail(DG_BAD_ARG, "null argument");
+  *kept = a->stored ? 1 : 0;
+  return DG_OK;
+}
+
 // forward run from the solver's state: nsteps SSP-RK3 steps of fixed dt,
 // h sampled at the receivers after every `every` steps, the state saved
 // every `ckpt` steps; samples = nsteps/every x nrec
@@ -1651,16 +1680,51 @@ extern "C" dg_status dg_adjoint_forward(dg_adjoint *a, int nsteps, double dt, in
   a->ckpt = ckpt;
   a->dt = dt;
   a->t0 = t0;
+  if (!a->ufinal && (st = amalloc(a, &a->ufinal, s->ndof_p)) != DG_OK) return st;
+  // keep every stage state when that fits in free device memory (leaving
+  // 4 GiB for everything else); otherwise the checkpoints alone
+  const size_t need = (size_t)3 * nsteps * s->ndof_p;
+  a->stored = false;
+  if (a->keep) {
+    if (a->store && a->store_n < need) {
+      cudaFree(a->store);
+      a->mem.erase(std::find(a->mem.begin(), a->mem.end(), (void *)a->store));
+      a->store = nullptr;
+      a->store_n = 0;
+    }
+    if (!a->store) {
+      size_t fr = 0, tot = 0;
+      if (cudaMemGetInfo(&fr, &tot) == cudaSuccess && need * sizeof(double) + ((size_t)4 << 30) < fr) {
+        void *q = nullptr;
+        if (cudaMalloc(&q, need * sizeof(double)) == cudaSuccess) {
+          a->mem.push_back(q);
+          a->store = static_cast<double *>(q);
+          a->store_n = need;
+        } else {
+          cudaGetLastError();  // not enough after all: checkpoints only
+        }
+      }
+    }
+    a->stored = a->store != nullptr;
+  }
   if ((st = set_fixed_dt(s, t0, dt)) != DG_OK) return st;
   const size_t bytes = s->ndof_p * sizeof(double);
   for (int n = 0; n < nsteps; n++) {
     if (n % ckpt == 0)
       CK(cudaMemcpyAsync(a->cks[n / ckpt], s->U, bytes, cudaMemcpyDeviceToDevice, s->st));
-    plain_step(s, nullptr, nullptr, n == 0);
+    if (a->stored) {
+      double *u = a->store + (size_t)3 * n * s->ndof_p;
+      CK(cudaMemcpyAsync(u, s->U, bytes, cudaMemcpyDeviceToDevice, s->st));
+      plain_step(s, u + s->ndof_p, u + 2 * s->ndof_p, n == 0);
+    } else {
+      plain_step(s, nullptr, nullptr, n == 0);
+    }
     if ((n + 1) % every == 0)
       dg::launch_sample(s->st, s->U, a->rec_el, a->rec_phi, a->nrec, s->np, s->m.Kp,
                         a->samples + (size_t)((n + 1) / every - 1) * a->nrec);
   }
+  CK(cudaMemcpyAsync(a->ufinal, s->U, bytes, cudaMemcpyDeviceToDevice, s->st));
+  CK(cudaMemcpyAsync(&a->t_end, &s->ds->t, sizeof(double), cudaMemcpyDeviceToHost, s->st));
   if (samples && nsamp && a->nrec)
     CK(cudaMemcpyAsync(samples, a->samples, sizeof(double) * nsamp * a->nrec,
                        cudaMemcpyDeviceToHost, s->st));
@@ -1699,13 +1763,15 @@ extern "C" dg_status dg_adjoint_backward(dg_adjoint *a, const double *sbar, doub
   const int nck = (int)a->cks.size();
   for (int k = nck - 1; k >= 0; k--) {
     const int n0 = k * a->ckpt, n1 = std::min(n0 + a->ckpt, a->nsteps);
-    // recompute the segment, keeping u^n, u1, u2 of every step
-    CK(cudaMemcpyAsync(s->U, a->cks[k], bytes, cudaMemcpyDeviceToDevice, s->st));
-    if ((st = set_fixed_dt(s, a->t0 + n0 * dt, dt)) != DG_OK) return st;
-    for (int m = n0; m < n1; m++) {
-      const int j = m - n0;
-      CK(cudaMemcpyAsync(a->seg[3 * j], s->U, bytes, cudaMemcpyDeviceToDevice, s->st));
-      plain_step(s, a->seg[3 * j + 1], a->seg[3 * j + 2], m == n0);
+    if (!a->stored) {
+      // recompute the segment, keeping u^n, u1, u2 of every step
+      CK(cudaMemcpyAsync(s->U, a->cks[k], bytes, cudaMemcpyDeviceToDevice, s->st));
+      if ((st = set_fixed_dt(s, a->t0 + n0 * dt, dt)) != DG_OK) return st;
+      for (int m = n0; m < n1; m++) {
+        const int j = m - n0;
+        CK(cudaMemcpyAsync(a->seg[3 * j], s->U, bytes, cudaMemcpyDeviceToDevice, s->st));
+        plain_step(s, a->seg[3 * j + 1], a->seg[3 * j + 2], m == n0);
+      }
     }
     for (int m = n1 - 1; m >= n0; m--) {
       const int j = m - n0;
@@ -1713,6 +1779,11 @@ extern "C" dg_status dg_adjoint_backward(dg_adjoint *a, const double *sbar, doub
         dg::launch_sample_adj(s->st, a->ub, a->rec_el, a->rec_phi, a->nrec, s->np, s->m.Kp,
                               a->sbar + (size_t)((m + 1) / a->every - 1) * a->nrec);
       double *un = a->seg[3 * j], *u1 = a->seg[3 * j + 1], *u2 = a->seg[3 * j + 2];
+      if (a->stored) {
+        un = a->store + (size_t)3 * m * s->ndof_p;
+        u1 = un + s->ndof_p;
+        u2 = un + 2 * s->ndof_p;
+      }
       // u^{n+1} = 1/3 u^n + 2/3 u2 + 2/3 dt L(u2)
       adj_stage(s, u2, a->ub, a->ub2, a->bbar, 2.0 / 3.0, 2.0 / 3.0 * dt, lb);
       dg::launch_axpby(s->st, n, 1.0 / 3.0, a->ub, 0.0, a->acc);
@@ -1736,11 +1807,9 @@ extern "C" dg_status dg_adjoint_backward(dg_adjoint *a, const double *sbar, doub
     CK(cudaMemcpyAsync(grad_b, s->ubuf, sizeof(double) * s->np * s->K, cudaMemcpyDeviceToHost,
                        s->st));
   }
-  // leave the solver at the final state of the forward run
-  CK(cudaMemcpyAsync(s->U, a->cks[nck - 1], bytes, cudaMemcpyDeviceToDevice, s->st));
-  if ((st = set_fixed_dt(s, a->t0 + (nck - 1) * a->ckpt * dt, dt)) != DG_OK) return st;
-  for (int m = (nck - 1) * a->ckpt; m < a->nsteps; m++)
-    plain_step(s, nullptr, nullptr, m == (nck - 1) * a->ckpt);
+  // leave the solver at the final state (and time) of the forward run
+  CK(cudaMemcpyAsync(s->U, a->ufinal, bytes, cudaMemcpyDeviceToDevice, s->st));
+  if ((st = set_fixed_dt(s, a->t_end, dt)) != DG_OK) return st;
   collect_profile(s);
   return sync_check(s);
 }

@@ -306,6 +306,15 @@ dg_status dg_adjoint_create(dg_solver *s, int nrec, const double *rx, const doub
                             dg_adjoint **out);
 dg_status dg_adjoint_forward(dg_adjoint *a, int nsteps, double dt, int every, int ckpt,
                              double t0, double *samples);
+/* What dg_adjoint_forward keeps for the reverse sweep: keep_stages = 0, the
+ * checkpoints only (each segment is recomputed by dg_adjoint_backward); 1
+ * (the default), also the three stage states u^n, u1, u2 of every step,
+ * 3 * nsteps states of the solver's size, when they fit in free device
+ * memory with 4 GiB to spare -- then the reverse sweep recomputes nothing --
+ * and the checkpoints only otherwise.  dg_adjoint_stored: *kept = 1 when the
+ * last forward run kept the stage states. */
+dg_status dg_adjoint_set_storage(dg_adjoint *a, int keep_stages);
+dg_status dg_adjoint_stored(const dg_adjoint *a, int *kept);
 dg_status dg_adjoint_backward(dg_adjoint *a, const double *sbar, double *grad_u0,
                               double *grad_b);
 dg_status dg_adjoint_tangent(dg_adjoint *a, const double *du0, const double *db,
