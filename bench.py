@@ -181,6 +181,7 @@ def ensemble_bench(device, nprob, steps, warmup, seed=4000):
         s.init_conditions()
     batch = dg.Batch(members)
     block = batch.autotune()
+    shared_blk, group_blk = batch.blocks()
     for s in members:
         s.init_conditions()
     tb = batch.step(warmup)
@@ -198,7 +199,10 @@ def ensemble_bench(device, nprob, steps, warmup, seed=4000):
     return {"problems": nprob, "triangles": tri, "dofs": ndof, "steps": steps,
             "value_batched": units / bat, "value_one_at_a_time": units / one,
             "ratio": one / bat, "identical": h_one == h_bat and list(tb) == list(t),
-            "batched_launches": launches, "autotuned_block": block, "unit": UNIT,
+            "batched_launches": launches, "autotuned_block": block,
+            "autotuned_element_blocks": {"p%d_%s" % (1 + g // 2, "large" if g % 2 else "small"): b
+                                         for g, b in enumerate(group_blk)},
+            "unit": UNIT,
             "note": "wall clock, synchronised; one-at-a-time = each member's own graph-"
                     "captured dg_step in sequence"}
 
@@ -388,7 +392,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--ensemble", type=int, default=256,
                     help="problems in the batched shallow-water ensemble (0: skip)")
-    ap.add_argument("--ensemble-steps", type=int, default=5)
+    ap.add_argument("--ensemble-steps", type=int, default=500)
     ap.add_argument("--adjoint-steps", type=int, default=2000,
                     help="steps of the shallow-water adjoint run (0: skip)")
     ap.add_argument("--adjoint-fd-dirs", type=int, default=16,

@@ -123,7 +123,9 @@ def _declare(L):
         "dg_bathymetry_project": (C.c_int, [C.c_void_p, C.c_int, _dp]),
         "dg_get_bathymetry": (C.c_int, [C.c_void_p, _dp]),
         "dg_autotune": (C.c_int, [C.c_void_p, _ip]),
+        "dg_autotune_stage": (C.c_int, [C.c_void_p, _ip, _ip]),
         "dg_batch_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
+        "dg_batch_blocks": (C.c_int, [C.c_void_p, _ip]),
         "dg_batch_step": (C.c_int, [C.c_void_p, C.c_int, _dp]),
         "dg_batch_autotune": (C.c_int, [C.c_void_p, _ip]),
         "dg_batch_launches": (C.c_longlong, [C.c_void_p]),
@@ -163,6 +165,13 @@ class Batch:
         tt = np.zeros(len(self.solvers)) if t is None else np.array(t, dtype=np.float64)
         _check(self._L.dg_batch_step(self._h, nsteps, _dptr(tt)))
         return tt
+
+    def blocks(self):
+        """(shared block size, element-stage block size of each (order,
+        mesh-size) group: 2 (p - 1) + (K >= 16384))."""
+        v = np.zeros(7, dtype=np.int32)
+        _check(self._L.dg_batch_blocks(self._h, _iptr(v)))
+        return int(v[0]), [int(x) for x in v[1:]]
 
     def autotune(self):
         b = C.c_int()
@@ -566,10 +575,26 @@ class Solver:
         a = np.ascontiguousarray(prm, dtype=np.float64)
         _check(self._L.dg_bathymetry_project(self._h, k, _dptr(a)))
 
+    def blocks(self):
+        """(shared block size, element-stage block size of each (order,
+        mesh-size) group: 2 (p - 1) + (K >= 16384))."""
+        v = np.zeros(7, dtype=np.int32)
+        _check(self._L.dg_batch_blocks(self._h, _iptr(v)))
+        return int(v[0]), [int(x) for x in v[1:]]
+
     def autotune(self):
         b = C.c_int()
         _check(self._L.dg_autotune(self._h, C.byref(b)))
         return b.value
+
+    def autotune_stage(self):
+        """(block size, threads per element): the stage kernels' block size
+        and, where the solver has both, the element stage (1: FP64 FMAs, one
+        thread per element; 2: tensor cores, a lane quad per two elements),
+        chosen by timing SSP-RK3 steps; the state is restored."""
+        b, tpe = C.c_int(), C.c_int()
+        _check(self._L.dg_autotune_stage(self._h, C.byref(b), C.byref(tpe)))
+        return b.value, tpe.value
 
     def rhs_tl(self, c, dc, db=None, t=0.0):
         """Tangent-linear right-hand side (shallow water)."""

@@ -849,8 +849,9 @@ __device__ __forceinline__ ElemArgs batch_elem_args(const BatchProb &pr, int sta
 }
 
 // the fused element stage of a batch, over the blocks [b_lo, b_lo +
-// gridDim.x) of the problems of one order P (the block map lists the
-// problems by order): one launch per order, each at its own register count
+// gridDim.x) of the problems of one order P and one mesh-size group (the
+// block map lists the problems by group): one launch per group, each at its
+// own register count and block size
 template <class Eq, int P>
 __global__ void __launch_bounds__(kMaxBlock)
     k_element_batch_p(const __grid_constant__ Tab<P> tab, const BatchProb *__restrict__ probs,
@@ -1081,7 +1082,7 @@ struct Launch {
     return *reinterpret_cast<const BatchTabs *>(b.tabs);
   }
   static void b_trace(const BatchLaunch &b) {
-    k_trace_batch<Eq><<<b.neblk, b.blk, 0, b.st>>>(btabs(b), b.probs, b.eblk2prob, b.eblk0);
+    k_trace_batch<Eq><<<b.nublk, b.blk, 0, b.st>>>(btabs(b), b.probs, b.ublk2prob, b.ublk0);
   }
   static void b_face(const BatchLaunch &b, double tcoef) {
     k_face_batch<Eq><<<b.nsblk, b.blk, 0, b.st>>>(btabs(b), b.probs, b.sblk2prob, b.sblk0,
@@ -1090,22 +1091,23 @@ struct Launch {
   static void b_element(const BatchLaunch &b, int stage) {
     const BatchTabs &tb = btabs(b);
     const int check = b.limiter ? 0 : 1;
-    for (int p = 1; p <= 3; p++) {  // the blocks are grouped by order
-      const int lo = b.eblk_p[p], n = b.eblk_p[p + 1] - lo;
+    // one launch per (order, mesh-size) group, each with its own block size
+    for (int g = 0; g < BatchLaunch::kGroups; g++) {
+      const int lo = b.eblk_g[g], n = b.eblk_g[g + 1] - lo, p = 1 + g / 2, blk = b.blk_g[g];
       if (n <= 0) continue;
       if (p == 1)
-        k_element_batch_p<Eq, 1><<<n, b.blk, 0, b.st>>>(tb.t1, b.probs, b.eblk2prob, b.eblk0, lo,
-                                                          stage, check);
+        k_element_batch_p<Eq, 1><<<n, blk, 0, b.st>>>(tb.t1, b.probs, b.eblk2prob, b.eblk0, lo,
+                                                        stage, check);
       else if (p == 2)
-        k_element_batch_p<Eq, 2><<<n, b.blk, 0, b.st>>>(tb.t2, b.probs, b.eblk2prob, b.eblk0, lo,
-                                                          stage, check);
+        k_element_batch_p<Eq, 2><<<n, blk, 0, b.st>>>(tb.t2, b.probs, b.eblk2prob, b.eblk0, lo,
+                                                        stage, check);
       else
-        k_element_batch_p<Eq, 3><<<n, b.blk, 0, b.st>>>(tb.t3, b.probs, b.eblk2prob, b.eblk0, lo,
-                                                          stage, check);
+        k_element_batch_p<Eq, 3><<<n, blk, 0, b.st>>>(tb.t3, b.probs, b.eblk2prob, b.eblk0, lo,
+                                                        stage, check);
     }
   }
   static void b_limit_tr(const BatchLaunch &b, int stage) {
-    k_limit_tr_batch<Eq><<<b.neblk, b.blk, 0, b.st>>>(btabs(b), b.probs, b.eblk2prob, b.eblk0,
+    k_limit_tr_batch<Eq><<<b.nublk, b.blk, 0, b.st>>>(btabs(b), b.probs, b.ublk2prob, b.ublk0,
                                                        stage);
   }
   static void b_lambda(const BatchLaunch &b) {

@@ -89,13 +89,17 @@ struct BatchLaunch {
   const void *tabs = nullptr;       // BatchTabs image (Tab<1>, Tab<2>, Tab<3>)
   BatchProb *probs = nullptr;       // device array
   int nprob = 0, blk = 128, limiter = 0;
-  const int *eblk2prob = nullptr, *eblk0 = nullptr;  // element blocks of size blk
+  // element blocks of the element stage: group g = 2 (p - 1) + (K >= 16384)
+  // holds the members of order p on small (0) or large (1) meshes, in blocks
+  // of blk_g[g] elements, the blocks [eblk_g[g], eblk_g[g + 1])
+  const int *eblk2prob = nullptr, *eblk0 = nullptr;
+  const int *ublk2prob = nullptr, *ublk0 = nullptr;  // element blocks of size blk (trace, limit)
   const int *sblk2prob = nullptr, *sblk0 = nullptr;  // side blocks of size blk
   const int *lblk2prob = nullptr, *lblk0 = nullptr;  // element blocks of 128 (wave speed)
-  int neblk = 0, nsblk = 0, nlblk = 0;
-  // element blocks of order p are [eblk_p[p], eblk_p[p + 1]), p = 1..3 (the
-  // map lists the problems by order)
-  int eblk_p[5] = {0, 0, 0, 0, 0};
+  int neblk = 0, nublk = 0, nsblk = 0, nlblk = 0;
+  static constexpr int kGroups = 6;
+  int eblk_g[kGroups + 1] = {0, 0, 0, 0, 0, 0, 0};
+  int blk_g[kGroups] = {128, 128, 128, 128, 128, 128};
 };
 
 struct BatchOps {

@@ -1040,15 +1040,11 @@ dg_status time_steps(cudaStream_t st, F &&step, float *ms) {
 const int kTuneBlocks[] = {64, 128, 256};
 }  // namespace
 
-extern "C" dg_status dg_autotune(dg_solver *s, int *block) {
-  if (!s) return fail(DG_BAD_ARG, "null solver");
-  s->tr_valid = false;
-  CK(cudaSetDevice(s->device));
-  double *save = nullptr;
-  CK(cudaMalloc(&save, s->ndof_p * sizeof(double)));
-  CK(cudaMemcpyAsync(save, s->U, s->ndof_p * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
-  int best = s->ctx.blk;
-  float best_ms = 1e30f;
+namespace {
+// times SSP-RK3 steps from the state `save` at each block size of the stage
+// kernels; the best block and its time
+dg_status tune_blocks(dg_solver *s, const double *save, int *best, float *best_ms) {
+  *best_ms = 1e30f;
   for (int blk : kTuneBlocks) {
     s->ctx.blk = blk;
     drop_graphs(s);
@@ -1060,20 +1056,59 @@ extern "C" dg_status dg_autotune(dg_solver *s, int *block) {
                       &ms);
     cudaMemcpyAsync(s->U, save, s->ndof_p * sizeof(double), cudaMemcpyDeviceToDevice, s->st);
     s->tr_valid = false;  // T belongs to the advanced state
+    if (st != DG_OK) return st;
+    if (ms < *best_ms) {
+      *best_ms = ms;
+      *best = blk;
+    }
+  }
+  return DG_OK;
+}
+}  // namespace
+
+extern "C" dg_status dg_autotune(dg_solver *s, int *block) {
+  return dg_autotune_stage(s, block, nullptr);
+}
+
+// threads_per_element == nullptr: block size only, with the element stage
+// as it is; else also the element stage itself where there is a choice
+extern "C" dg_status dg_autotune_stage(dg_solver *s, int *block, int *threads_per_element) {
+  if (!s) return fail(DG_BAD_ARG, "null solver");
+  s->tr_valid = false;
+  CK(cudaSetDevice(s->device));
+  double *save = nullptr;
+  CK(cudaMalloc(&save, s->ndof_p * sizeof(double)));
+  CK(cudaMemcpyAsync(save, s->U, s->ndof_p * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
+  std::vector<int> variants;  // 1: the FP64 element stage, 2: the tensor-core one
+  if (threads_per_element && s->oz) variants = {1, 2};
+  else variants = {s->ctx.oz ? 2 : 1};
+  int best_blk = s->ctx.blk, best_v = variants[0];
+  float best_ms = 1e30f;
+  for (int v : variants) {
+    s->tensor = v == 2;
+    s->ctx.oz = s->tensor ? s->oz : nullptr;
+    int blk = s->ctx.blk;
+    float ms = 0;
+    dg_status st = tune_blocks(s, save, &blk, &ms);
     if (st != DG_OK) {
+      cudaStreamSynchronize(s->st);
       cudaFree(save);
       return st;
     }
     if (ms < best_ms) {
       best_ms = ms;
-      best = blk;
+      best_blk = blk;
+      best_v = v;
     }
   }
   cudaStreamSynchronize(s->st);
   cudaFree(save);
-  s->ctx.blk = best;
+  s->tensor = best_v == 2;
+  s->ctx.oz = s->tensor ? s->oz : nullptr;
+  s->ctx.blk = best_blk;
   drop_graphs(s);
-  if (block) *block = best;
+  if (block) *block = best_blk;
+  if (threads_per_element) *threads_per_element = best_v;
   return DG_OK;
 }
 
@@ -1116,51 +1151,63 @@ void block_maps(const std::vector<int> &count, const std::vector<int> &order, in
   }
 }
 
+// the element-stage group of a member: order and mesh size
+constexpr int kSmallMesh = 16384;
+int batch_group(const dg_solver *s) { return 2 * (s->p - 1) + (s->K >= kSmallMesh ? 1 : 0); }
+
 dg_status batch_build_maps(dg_batch *b) {
   std::vector<int> ke, ks;
   for (auto *s : b->m) {
     ke.push_back(s->K);
     ks.push_back(s->S);
   }
-  // problems of one order next to each other, so that the blocks resident
-  // on an SM at a time mostly run the same order's code (the kernels switch
-  // on p per block); within an order, larger problems first
+  // problems of one group (order, mesh size) next to each other, so that the
+  // element stage is one launch per group at its own block size and register
+  // count; within a group, larger problems first
   std::vector<int> order(b->m.size());
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
-    if (b->m[x]->p != b->m[y]->p) return b->m[x]->p < b->m[y]->p;
+    const int gx = batch_group(b->m[x]), gy = batch_group(b->m[y]);
+    if (gx != gy) return gx < gy;
     return b->m[x]->K > b->m[y]->K;
   });
-  std::vector<int> e2p, e0, s2p, s0, l2p, l0;
-  block_maps(ke, order, b->blk, e2p, e0);
+  dg::BatchLaunch &L = b->bl;
+  std::vector<int> e2p, e0(b->m.size(), 0), u2p, u0, s2p, s0, l2p, l0;
+  for (int g = 0; g < dg::BatchLaunch::kGroups; g++) {
+    L.eblk_g[g] = (int)e2p.size();
+    for (int i : order) {
+      if (batch_group(b->m[i]) != g) continue;
+      e0[i] = (int)e2p.size();
+      const int nb = (ke[i] + L.blk_g[g] - 1) / L.blk_g[g];
+      for (int k = 0; k < nb; k++) e2p.push_back(i);
+    }
+  }
+  L.eblk_g[dg::BatchLaunch::kGroups] = (int)e2p.size();
+  block_maps(ke, order, b->blk, u2p, u0);
   block_maps(ks, order, b->blk, s2p, s0);
   block_maps(ke, order, 128, l2p, l0);
   std::vector<int> all;
-  size_t oe2p = 0, oe0 = oe2p + e2p.size(), os2p = oe0 + e0.size(), os0 = os2p + s2p.size(),
-         ol2p = os0 + s0.size(), ol0 = ol2p + l2p.size();
-  for (auto *v : {&e2p, &e0, &s2p, &s0, &l2p, &l0}) all.insert(all.end(), v->begin(), v->end());
+  size_t oe2p = 0, oe0 = oe2p + e2p.size(), ou2p = oe0 + e0.size(), ou0 = ou2p + u2p.size(),
+         os2p = ou0 + u0.size(), os0 = os2p + s2p.size(), ol2p = os0 + s0.size(),
+         ol0 = ol2p + l2p.size();
+  for (auto *v : {&e2p, &e0, &u2p, &u0, &s2p, &s0, &l2p, &l0})
+    all.insert(all.end(), v->begin(), v->end());
   if (b->maps) cudaFree(b->maps);
   b->maps = nullptr;
   CK(cudaMalloc(&b->maps, all.size() * sizeof(int)));
   CK(cudaMemcpy(b->maps, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice));
-  dg::BatchLaunch &L = b->bl;
   L.eblk2prob = b->maps + oe2p;
   L.eblk0 = b->maps + oe0;
+  L.ublk2prob = b->maps + ou2p;
+  L.ublk0 = b->maps + ou0;
   L.sblk2prob = b->maps + os2p;
   L.sblk0 = b->maps + os0;
   L.lblk2prob = b->maps + ol2p;
   L.lblk0 = b->maps + ol0;
   L.neblk = (int)e2p.size();
+  L.nublk = (int)u2p.size();
   L.nsblk = (int)s2p.size();
   L.nlblk = (int)l2p.size();
-  // element-block ranges of orders 1..3 (contiguous: `order` sorts by p;
-  // batch creation admits p = 1..3 only)
-  int cnt[4] = {0, 0, 0, 0};
-  for (auto *sv : b->m) cnt[sv->p] += (sv->K + b->blk - 1) / b->blk;
-  L.eblk_p[1] = 0;
-  L.eblk_p[2] = cnt[1];
-  L.eblk_p[3] = cnt[1] + cnt[2];
-  L.eblk_p[4] = cnt[1] + cnt[2] + cnt[3];
   L.blk = b->blk;
   if (b->graph) cudaGraphExecDestroy(b->graph);
   b->graph = nullptr;
@@ -1312,6 +1359,10 @@ extern "C" dg_status dg_batch_step(dg_batch *b, int nsteps, double *t) {
   return batch_run(b, nsteps, t);
 }
 
+// Block sizes of a batch, timed on SSP-RK3 steps from the members' current
+// states (restored afterwards): first the one shared by the face, trace and
+// limiter launches, then each element-stage group's (order, mesh size) in
+// turn, each trying 64, 128 and 256 elements per block.
 extern "C" dg_status dg_batch_autotune(dg_batch *b, int *block) {
   if (!b) return fail(DG_BAD_ARG, "null batch");
   CK(cudaSetDevice(b->device));
@@ -1321,31 +1372,48 @@ extern "C" dg_status dg_batch_autotune(dg_batch *b, int *block) {
     CK(cudaMemcpy(save[i], b->m[i]->U, b->m[i]->ndof_p * sizeof(double),
                   cudaMemcpyDeviceToDevice));
   }
-  int best = b->blk;
-  float best_ms = 1e30f;
+  bool used[dg::BatchLaunch::kGroups] = {false};
+  for (auto *s : b->m) used[batch_group(s)] = true;
   std::vector<double> t(b->m.size(), 0.0);
   dg_status st = DG_OK;
-  for (int blk : kTuneBlocks) {
-    b->blk = blk;
-    if ((st = batch_build_maps(b)) != DG_OK) break;
-    if ((st = batch_run(b, 1, t.data())) != DG_OK) break;
-    float ms = 0;
-    st = time_steps(b->st, [&] { return batch_run(b, 3, t.data()); }, &ms);
+  // times 3 steps with the current settings
+  auto trial = [&](float *ms) -> dg_status {
+    dg_status r = batch_build_maps(b);
+    if (r == DG_OK) r = batch_run(b, 1, t.data());  // capture + warm
+    if (r == DG_OK) r = time_steps(b->st, [&] { return batch_run(b, 3, t.data()); }, ms);
     for (size_t i = 0; i < b->m.size(); i++)
       cudaMemcpy(b->m[i]->U, save[i], b->m[i]->ndof_p * sizeof(double),
                  cudaMemcpyDeviceToDevice);
-    if (st != DG_OK) break;
-    if (ms < best_ms) {
-      best_ms = ms;
-      best = blk;
+    return r;
+  };
+  for (int knob = -1; knob < dg::BatchLaunch::kGroups && st == DG_OK; knob++) {
+    if (knob >= 0 && !used[knob]) continue;
+    int &v = knob < 0 ? b->blk : b->bl.blk_g[knob];
+    int best = v;
+    float best_ms = 1e30f;
+    for (int blk : kTuneBlocks) {
+      v = blk;
+      float ms = 0;
+      if ((st = trial(&ms)) != DG_OK) break;
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = blk;
+      }
     }
+    v = best;
   }
   for (auto *p : save) cudaFree(p);
   if (st != DG_OK) return st;
-  b->blk = best;
   st = batch_build_maps(b);
-  if (block) *block = best;
+  if (block) *block = b->blk;
   return st;
+}
+
+extern "C" dg_status dg_batch_blocks(const dg_batch *b, int *blocks) {
+  if (!b || !blocks) return fail(DG_BAD_ARG, "null argument");
+  blocks[0] = b->blk;
+  for (int g = 0; g < dg::BatchLaunch::kGroups; g++) blocks[1 + g] = b->bl.blk_g[g];
+  return DG_OK;
 }
 
 extern "C" long long dg_batch_launches(const dg_batch *b) { return b ? b->launches : 0; }

@@ -265,12 +265,19 @@ dg_status dg_bathymetry_project(dg_solver *s, int kind, const double *prm);
  * kernels, chosen by timing SSP-RK3 steps with 64, 128 and 256; the state is
  * restored afterwards.  *block receives the choice. */
 dg_status dg_autotune(dg_solver *s, int *block);
+/* dg_autotune that also chooses the element stage, where a solver has two:
+ * the FP64-FMA kernel, one thread per element, or the tensor-core kernel,
+ * whose quad of lanes holds two elements (two threads per element; Euler,
+ * p = 1..4).  *threads_per_element receives 1 or 2.  The two agree to FP64
+ * rounding, not bit for bit, so a run's last bits follow the choice. */
+dg_status dg_autotune_stage(dg_solver *s, int *block, int *threads_per_element);
 
 /* ---- batched ensembles: independent problems stepped together -----------
- * One launch per kernel per RK stage covers every member (concatenated
- * element ranges; each member keeps its own mesh, order p in 1..3, CFL time
- * step and time), and one SSP-RK3 step of the whole ensemble is one CUDA
- * graph.  Members must share device, equation and limiter setting; they
+ * Per RK stage one face launch covers every member (concatenated element
+ * and side ranges; each member keeps its own mesh, order p in 1..3, CFL time
+ * step and time) and the element stage is one launch per group of members
+ * of one order and mesh-size class (dg_batch_autotune); one SSP-RK3 step of
+ * the whole ensemble is one CUDA graph.  Members must share device, equation and limiter setting; they
  * stay owned by the caller and must outlive the batch.  No reference
  * counterpart (DGCUDA runs one problem per process). */
 typedef struct dg_batch dg_batch;
@@ -278,7 +285,14 @@ dg_status dg_batch_create(int n, dg_solver *const *members, dg_batch **out);
 /* nsteps SSP-RK3 steps of every member; t[i] is member i's time (read and
  * advanced) */
 dg_status dg_batch_step(dg_batch *b, int nsteps, double *t);
+/* block sizes of the batch's launches, timed on SSP-RK3 steps (states
+ * restored): the one shared by the face, trace and limiter launches (*block),
+ * then the element stage's per group -- group g = 2 (p - 1) + (K >= 16384):
+ * members of order p on meshes below or from 16384 triangles, each its own
+ * launch -- each from 64, 128 and 256 elements per block */
 dg_status dg_batch_autotune(dg_batch *b, int *block);
+/* blocks[0] = the shared block size, blocks[1 + g] = group g's (7 ints) */
+dg_status dg_batch_blocks(const dg_batch *b, int *blocks);
 long long dg_batch_launches(const dg_batch *b);
 void dg_batch_destroy(dg_batch *b);
 

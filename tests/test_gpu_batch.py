@@ -1,5 +1,6 @@
-"""Batched ensembles (one launch per kernel per stage for all members),
-the shallow-water bed source, and the block-size autotuner."""
+"""Batched ensembles (per stage one face launch for all members, one
+element launch per (order, mesh-size) group), the shallow-water bed source,
+and the autotuners."""
 import numpy as np
 import pytest
 
@@ -114,14 +115,45 @@ def test_autotune_keeps_results(dglib):
 
 
 def test_batch_autotune_keeps_results(dglib):
+    """Block sizes tuned per (order, mesh-size) group of the element stage:
+    the results stay those of the untuned batch and of the members stepped
+    one at a time."""
     from dgcuda_gb300.ensemble import build_member, ensemble_specs
     dg = dglib
-    specs = ensemble_specs(5, seed=3, tri_min=500, tri_max=5000)
+    specs = ensemble_specs(8, seed=3, tri_min=2000, tri_max=40000)
     a = [build_member(sp) for sp in specs]
     b = [build_member(sp) for sp in specs]
+    c = [build_member(sp) for sp in specs]
+    assert {s.K >= 16384 for s in a} == {False, True}
     ba = dg.Batch(a)
     assert ba.autotune() in (64, 128, 256)
+    shared, groups = ba.blocks()
+    assert shared in (64, 128, 256) and all(g in (64, 128, 256) for g in groups)
     ba.step(4)
     dg.Batch(b).step(4)
-    for sa, sb in zip(a, b):
+    for s in c:
+        s.step(4, dg.SSP_RK3, 0.0)
+    for sa, sb, sc in zip(a, b, c):
         assert np.array_equal(sa.get_state(), sb.get_state())
+        assert np.array_equal(sa.get_state(), sc.get_state())
+
+
+def test_autotune_stage_choice_restores_state_and_matches_oracle(dglib, oracle_mod):
+    """Euler p = 3 with the limiter: the tuner picks a block size and the
+    element stage (threads per element 1: FP64, 2: tensor cores), restores
+    the state, and the run it leaves matches the oracle."""
+    dg = dglib
+    m = dg.Mesh.square(64, 64, jitter=0.1, seed=3, bc=(-4, -4, -4, -4))
+    s = dg.Solver(m, dg.EULER, 3, problem="euler_riemann4", limiter=1, cfl=0.2)
+    s.init_conditions()
+    c0 = s.get_state()
+    blk, tpe = s.autotune_stage()
+    assert blk in (64, 128, 256) and tpe in (1, 2)
+    assert s.tensor_contractions == (tpe == 2)
+    assert np.array_equal(s.get_state(), c0)
+    t = s.step(5, dg.SSP_RK3, 0.0)
+    o = oracle_mod.Oracle.from_mesh(m, dg.EULER, 3, oracle_mod.prm_vec(gamma=1.4),
+                                    dg.PROBLEMS["euler_riemann4"])
+    c, to, _ = o.step(c0, 5, 0, 1, 0.2)
+    assert abs(t - to) <= 1e-12 * to
+    assert relerr(s.get_state(), c, 4) <= 1e-10
