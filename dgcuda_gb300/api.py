@@ -118,8 +118,6 @@ def _declare(L):
         "dg_set_tensor_contractions": (C.c_int, [C.c_void_p, C.c_int]),
         "dg_oz_table_image": (C.c_int, [C.c_int, C.c_void_p, C.c_size_t, _dp]),
         "dg_get_tensor_contractions": (C.c_int, [C.c_void_p, _ip]),
-        "dg_set_pipelined_stage": (C.c_int, [C.c_void_p, C.c_int]),
-        "dg_get_pipelined_stage": (C.c_int, [C.c_void_p, _ip]),
         "dg_load_checkpoint": (C.c_int, [C.c_void_p, C.c_char_p, _dp]),
         "dg_set_bathymetry": (C.c_int, [C.c_void_p, _dp]),
         "dg_bathymetry_project": (C.c_int, [C.c_void_p, C.c_int, _dp]),
@@ -509,18 +507,6 @@ class Solver:
     @tensor_contractions.setter
     def tensor_contractions(self, on):
         _check(self._L.dg_set_tensor_contractions(self._h, int(bool(on))))
-
-    @property
-    def pipelined_stage(self):
-        """True when an SSP-RK3 stage runs as one persistent launch (the
-        tensor-core Euler path; on by default there)."""
-        v = np.zeros(1, dtype=np.int32)
-        _check(self._L.dg_get_pipelined_stage(self._h, _iptr(v)))
-        return bool(v[0])
-
-    @pipelined_stage.setter
-    def pipelined_stage(self, on):
-        _check(self._L.dg_set_pipelined_stage(self._h, int(bool(on))))
 
     def set_velocity_field(self, ax, ay, grad=None):
         """Advection velocity a(x, y) = (ax, ay) + grad (x, y), grad =

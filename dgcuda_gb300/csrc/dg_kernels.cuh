@@ -442,10 +442,13 @@ __global__ void __launch_bounds__(kMaxBlock) k_element(const __grid_constant__ T
 // epilogue's roundings; the element stage writes these M as the output's
 // mode 0, so the limiter's neighbour bounds see exactly the stored means.
 template <class Eq, int P>
-__device__ __forceinline__ void means_body(const Tab<P> &tab, const ElemArgs &a,
-                                           const double *__restrict__ Fs, double *__restrict__ M,
-                                           int e) {
+__global__ void __launch_bounds__(kMaxBlock) k_means(const __grid_constant__ Tab<P> tab,
+                                                     const __grid_constant__ ElemArgs a,
+                                                     const double *__restrict__ Fs,
+                                                     double *__restrict__ M) {
   constexpr int N = Eq::N, NP = Tab<P>::NP;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= a.K) return;
   const size_t Kp = a.Kp;
   double sum[N];
 #pragma unroll
@@ -469,15 +472,6 @@ __device__ __forceinline__ void means_body(const Tab<P> &tab, const ElemArgs &a,
     if (a.ca != 0.0) v = fma(a.ca, a.un[o], v);
     M[(size_t)n * Kp + e] = v;
   }
-}
-
-template <class Eq, int P>
-__global__ void __launch_bounds__(kMaxBlock) k_means(const __grid_constant__ Tab<P> tab,
-                                                     const __grid_constant__ ElemArgs a,
-                                                     const double *__restrict__ Fs,
-                                                     double *__restrict__ M) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e < a.K) means_body<Eq, P>(tab, a, Fs, M, e);
 }
 
 // ---------------------------------------------------------------------------
@@ -997,23 +991,6 @@ struct Launch {
     DG_DISPATCH_P((k_trace<Eq, P><<<nblk(c.m.K, c.blk), c.blk, 0, c.st>>>(tab<P>(c), *c.q, u,
                                                                           c.T, c.m.K, c.m.Kp)));
   }
-  static FaceArgs fargs(const Ctx &c, const double *t, double tcoef, double *Fs) {
-    FaceArgs a;
-    a.T = c.T;
-    a.side = c.m.side;
-    a.sgeo = c.m.sgeo;
-    a.bxy = c.m.bxy;
-    a.vtx = c.m.vtx;
-    a.Fh = c.Fh;
-    a.Fs = Fs;
-    a.tptr = t;
-    a.dtp = &c.ds->dt;
-    a.tcoef = tcoef;
-    a.S = c.m.S;
-    a.Sb = c.m.Sb;
-    a.Kp = c.m.Kp;
-    return a;
-  }
   template <bool FS>
   static void face_args(const Ctx &c, const double *t, double tcoef, double *Fs) {
     if (!c.m.S) return;
@@ -1096,7 +1073,7 @@ struct Launch {
 
   static const Ops &ops() {
     static const Ops o = {trace,  face,       element,  limit,  lambda,  init,    l2err,
-                          element_tr, limit_tr, vertex, nullptr, nullptr, nullptr, nullptr};
+                          element_tr, limit_tr, vertex, nullptr, nullptr, nullptr};
     return o;
   }
 

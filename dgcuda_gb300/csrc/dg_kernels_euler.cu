@@ -37,20 +37,6 @@ void element_lim(const Ctx &c, double *us, const double *un, double *out, double
   oz_element(c, L::eargs(c, us, un, out, ca, cb, cc, dtp, c.T, 0), true);
 }
 
-// the whole stage as one persistent launch (the caller clears the work list)
-void stage_pipe(const Ctx &c, const double *t, double tcoef, double *us, const double *un,
-                double *out, double ca, double cb, double cc, const double *dtp, int lim) {
-  if (!c.m.K) return;
-  const ElemArgs a = L::eargs(c, us, un, out, ca, cb, cc, dtp, c.T, lim ? 0 : 1);
-  const FaceArgs fa = L::fargs(c, t, tcoef, lim ? c.Fs : nullptr);
-  switch (c.p) {
-    case 1: oz::euler_stage_pipe<1>(c, a, fa, lim); break;
-    case 2: oz::euler_stage_pipe<2>(c, a, fa, lim); break;
-    case 3: oz::euler_stage_pipe<3>(c, a, fa, lim); break;
-    case 4: oz::euler_stage_pipe<4>(c, a, fa, lim); break;
-  }
-}
-
 void trace(const Ctx &c, double *u) {
   if (!c.oz || c.p < 1 || c.p > 4) {
     L::trace(c, u);
@@ -72,7 +58,6 @@ Ops make_ops() {
   o.face_fs = L::face_fs;
   o.means = L::means;
   o.element_lim = element_lim;
-  o.stage_pipe = stage_pipe;
   return o;
 }
 
@@ -84,15 +69,14 @@ const Ops &ops_euler() {
 }
 const BatchOps &batch_ops_euler() { return Launch<Euler>::batch_ops(); }
 
-// allows the tensor-core element and pipelined-stage kernels of order p
-// their shared memory (once per device, before any capture); *per_sm:
-// resident blocks of the pipelined stage per SM
-cudaError_t oz_prepare_euler(int p, int *per_sm) {
+// allows the tensor-core element kernels of order p their shared memory
+// (once per device, before any capture)
+cudaError_t oz_prepare_euler(int p) {
   switch (p) {
-    case 1: return oz::euler_prepare<1>(per_sm);
-    case 2: return oz::euler_prepare<2>(per_sm);
-    case 3: return oz::euler_prepare<3>(per_sm);
-    case 4: return oz::euler_prepare<4>(per_sm);
+    case 1: return oz::euler_prepare<1>();
+    case 2: return oz::euler_prepare<2>();
+    case 3: return oz::euler_prepare<3>();
+    case 4: return oz::euler_prepare<4>();
     default: return cudaErrorInvalidValue;
   }
 }

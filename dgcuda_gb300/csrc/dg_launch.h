@@ -56,20 +56,6 @@ struct DevScalars {
   int last;         // 1 when this step was shortened to land on endtime
 };
 
-// The work list of a pipelined stage (one persistent launch per RK stage):
-// items in an order where each waits only on items before it
-struct PipeArgs {
-  const int *items = nullptr;  // type << 29 | tile; type 0 face, 1 means, 2 element
-  int nitems = 0;
-  int nface = 0;               // face tiles; the flags of the means tiles follow theirs
-  int nelem = 0;               // element (and means) tiles
-  int *work = nullptr;         // [0] next item, [1] error, [2..] flags (reset per launch)
-  const int *fdep_ptr = nullptr, *fdep = nullptr;  // per element tile: face tiles it needs
-  const int *mdep_ptr = nullptr, *mdep = nullptr;  // per element tile: means tiles it needs
-  int grid = 0;                // persistent blocks
-  int lim = 0;                 // the list's form: 1 with means items (limiter on)
-};
-
 struct Ctx {
   cudaStream_t st = nullptr;
   DevMesh m;
@@ -83,7 +69,6 @@ struct Ctx {
   double *M = nullptr;            // means of the stage output [var][Kp] (fused limiter)
   DevScalars *ds = nullptr;       // device scalars
   const void *oz = nullptr;       // tensor-core tables of order p (null: FP64 contractions)
-  PipeArgs pipe[2];               // pipelined-stage work lists without / with the limiter
 };
 
 // one problem of a batched ensemble (device resident)
@@ -170,11 +155,6 @@ struct Ops {
                 const double *dtp);
   void (*element_lim)(const Ctx &, double *us, const double *un, double *out, double ca,
                       double cb, double cc, const double *dtp);
-  // the whole stage (faces, means, element stage, limiter when lim) as one
-  // persistent launch over the work list Ctx::pipe[lim] (null where an
-  // equation has none); the caller clears pipe.work first
-  void (*stage_pipe)(const Ctx &, const double *t, double tcoef, double *us, const double *un,
-                     double *out, double ca, double cb, double cc, const double *dtp, int lim);
 };
 
 const Ops &ops_advection();
@@ -183,7 +163,7 @@ const Ops &ops_euler();
 // from the host Tab<p> image, and the per-device kernel attribute
 size_t oz_tabs_bytes();
 bool oz_build_tabs(int p, const void *tabimg, void *out, double *dense = nullptr);
-cudaError_t oz_prepare_euler(int p, int *pipe_blocks_per_sm);
+cudaError_t oz_prepare_euler(int p);
 const Ops &ops_shallow_water();
 const Ops &ops_maxwell();
 

@@ -428,21 +428,21 @@ __device__ __forceinline__ void limit_epilogue(const Tab<P> &tab, const ElemArgs
 // element and its three neighbours (a.nbr) give the bounds, and the limited
 // modes and traces -- limit_tr_body's rules -- are what is written; the
 // positivity rule is then applied to the limited traces (limit_epilogue).
-// the elements [64 tile, 64 tile + 64) of the stage, by the 128 threads of a
-// block (4 warps of 16 elements); smem_d: the block's oz_smem_bytes
-template <class Eq, int P, bool LIM>
-__device__ __forceinline__ void element_oz_tile(const Tab<P> &tab, const EqP &q,
-                                                const ElemArgs &a, const Tabs *__restrict__ ozt,
-                                                int tile, double *smem_d) {
+template <class Eq, int P, bool LIM = false>
+__global__ void __launch_bounds__(kOzThreads, P <= 3 ? 4 : 3) k_element_oz(const __grid_constant__ Tab<P> tab,
+                                                           const __grid_constant__ EqP q,
+                                                           const __grid_constant__ ElemArgs a,
+                                                           const Tabs *__restrict__ ozt) {
   static_assert(!Eq::kBathymetry, "bed source not provided on this path");
   using S = OzShape<Eq, P>;
   constexpr int N = S::N, NP = S::NP, NQ = S::NQ, N1 = S::N1, NF = S::NF;
   constexpr int PM = S::PM, PQ = S::PQ, PF = S::PF;
   static_assert(NP <= 16 && NQ <= 16 && NF <= 16, "p <= 4");
+  extern __shared__ __align__(16) double smem_d[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, t = lane & 3;
   double *gh = smem_d + (size_t)warp * S::GH * 32;
   const int K = a.K, Kp = a.Kp;
-  const int e0 = (tile * 4 + warp) * 16 + (lane >> 2);
+  const int e0 = (blockIdx.x * 4 + warp) * 16 + (lane >> 2);
   const int el[2] = {e0, e0 + 8};
   const bool live[2] = {el[0] < K, el[1] < K};
   const int ec[2] = {live[0] ? el[0] : K - 1, live[1] ? el[1] : K - 1};  // loads stay in bounds
@@ -823,15 +823,6 @@ __device__ __forceinline__ void element_oz_tile(const Tab<P> &tab, const EqP &q,
         }
     }
   }
-}
-
-template <class Eq, int P, bool LIM = false>
-__global__ void __launch_bounds__(kOzThreads, P <= 3 ? 4 : 3) k_element_oz(const __grid_constant__ Tab<P> tab,
-                                                           const __grid_constant__ EqP q,
-                                                           const __grid_constant__ ElemArgs a,
-                                                           const Tabs *__restrict__ ozt) {
-  extern __shared__ __align__(16) double smem_d[];
-  element_oz_tile<Eq, P, LIM>(tab, q, a, ozt, blockIdx.x, smem_d);
 }
 
 // Edge traces of a state with the tensor-core trace contraction (trace_body's

@@ -27,8 +27,8 @@ struct ProfEvent {
   int kind;
   cudaEvent_t a, b;
 };
-const char *kKindName[] = {"trace", "face", "element", "limit", "cfl", "rk", "means", "stage"};
-constexpr int kKinds = 8;
+const char *kKindName[] = {"trace", "face", "element", "limit", "cfl", "rk", "means"};
+constexpr int kKinds = 7;
 
 }  // namespace
 
@@ -47,11 +47,6 @@ struct dg_solver {
   double *U = nullptr, *W = nullptr, *k[4] = {nullptr, nullptr, nullptr, nullptr};
   double *ubuf = nullptr, *partial = nullptr, *T = nullptr, *Fh = nullptr, *vbuf = nullptr;
   double *Fs = nullptr, *M = nullptr;  // side-flux sums and output means (fused limiter)
-  // pipelined stage: work lists (without / with the limiter), their shared
-  // work buffer (next item, error word, flags), resident blocks per SM
-  int *pipe_work = nullptr;
-  int pipe_per_sm = 0;
-  bool pipelined = true;
   double *bathy = nullptr;        // bed modes (shallow water), internal order
   double *lin_tv = nullptr, *lin_f0 = nullptr, *lin_f1 = nullptr;  // adjoint work
   bool has_inout_bc = false;      // a side with an inflow or outflow code
@@ -163,10 +158,7 @@ void collect_profile(dg_solver *s) {
   s->pending.clear();
 }
 
-enum {
-  K_TRACE = 0, K_FACE = 1, K_ELEMENT = 2, K_LIMIT = 3, K_CFL = 4, K_RK = 5, K_MEANS = 6,
-  K_STAGE = 7
-};
+enum { K_TRACE = 0, K_FACE = 1, K_ELEMENT = 2, K_LIMIT = 3, K_CFL = 4, K_RK = 5, K_MEANS = 6 };
 
 // one RK stage of the DG operator: out = ca*un + cb*us + cc*dt*L(us).
 // With the tensor-core contractions on, the element stage is the one the
@@ -196,18 +188,6 @@ void limit(dg_solver *s, double *u) {
 void fused_stage(dg_solver *s, double *us, const double *un, double *out, double ca, double cb,
                  double cc, double tcoef, const double *dtp) {
   const bool lim = s->prm.limiter && s->np >= 3;
-  const dg::PipeArgs &pa = s->ctx.pipe[lim ? 1 : 0];
-  if (s->pipelined && s->ctx.oz && s->ops->stage_pipe && pa.items && pa.grid > 0 &&
-      (!lim || s->ctx.M)) {
-    // the whole stage as one persistent launch (dg_pipeline.cuh): clear
-    // the next-item counter and the items' flags (the error word stays)
-    run(s, K_STAGE, [&] {
-      cudaMemsetAsync(pa.work, 0, sizeof(int), s->st);
-      cudaMemsetAsync(pa.work + 2, 0, sizeof(int) * (size_t)(pa.nface + pa.nelem), s->st);
-      s->ops->stage_pipe(s->ctx, &s->ds->t, tcoef, us, un, out, ca, cb, cc, dtp, lim ? 1 : 0);
-    });
-    return;
-  }
   if (lim && s->ctx.oz && s->ops->element_lim && s->ctx.M) {
     run(s, K_FACE, [&] { s->ops->face_fs(s->ctx, &s->ds->t, tcoef); });
     run(s, K_MEANS, [&] { s->ops->means(s->ctx, us, un, ca, cb, cc, dtp); });
@@ -306,110 +286,6 @@ void drop_graphs(dg_solver *s) {
   s->graph_launches.clear();
 }
 
-// The work lists of the pipelined stage (dg_pipeline.cuh) from the
-// connectivity: face tiles of 128 sides, means and element tiles of 64
-// elements.  A means tile needs the face tiles of its elements' sides; an
-// element tile needs those (without the limiter) or the means tiles of its
-// elements and their neighbours (with it).  Each list puts every item after
-// all the items it needs: face tiles in order, each means tile right after
-// the last face tile it needs, each element tile right after the last item
-// it needs.
-dg_status pipe_build(dg_solver *s, const std::vector<int> &esd, const std::vector<int> &nbr) {
-  const int K = s->K, S = s->S, Kp = s->m.Kp;
-  const int FT = 128, ET = 64;
-  const int nface = (S + FT - 1) / FT, nelem = (K + ET - 1) / ET;
-  std::vector<int> fptr(nelem + 1, 0), fdep, mptr(nelem + 1, 0), mdep, maxf(nelem, 0);
-  for (int k = 0; k < nelem; k++) {
-    std::vector<int> fl, ml;
-    for (int e = k * ET; e < std::min(K, (k + 1) * ET); e++)
-      for (int f = 0; f < 3; f++) {
-        fl.push_back((esd[(size_t)f * Kp + e] >> 1) / FT);
-        ml.push_back(nbr[(size_t)f * Kp + e] / ET);
-      }
-    ml.push_back(k);
-    std::sort(fl.begin(), fl.end());
-    fl.erase(std::unique(fl.begin(), fl.end()), fl.end());
-    std::sort(ml.begin(), ml.end());
-    ml.erase(std::unique(ml.begin(), ml.end()), ml.end());
-    maxf[k] = fl.empty() ? 0 : fl.back();
-    fdep.insert(fdep.end(), fl.begin(), fl.end());
-    mdep.insert(mdep.end(), ml.begin(), ml.end());
-    fptr[k + 1] = (int)fdep.size();
-    mptr[k + 1] = (int)mdep.size();
-  }
-  std::vector<std::vector<int>> after_face(nface);  // tiles whose last face tile is j
-  for (int k = 0; k < nelem; k++) after_face[maxf[k]].push_back(k);
-  auto code = [](int type, int tile) { return (type << 29) | tile; };
-  // without the limiter: F_j, then the element tiles whose faces are done
-  std::vector<int> items0, items1;
-  for (int j = 0; j < nface; j++) {
-    items0.push_back(code(0, j));
-    for (int k : after_face[j]) items0.push_back(code(2, k));
-  }
-  // with it: F_j, the means tiles it completes, the element tiles those complete
-  std::vector<int> pending(nelem), rev_ptr(nelem + 1, 0), rev;
-  for (int k = 0; k < nelem; k++) pending[k] = mptr[k + 1] - mptr[k];
-  for (int k = 0; k < nelem; k++)
-    for (int i = mptr[k]; i < mptr[k + 1]; i++) rev_ptr[mdep[i] + 1]++;
-  for (int m = 0; m < nelem; m++) rev_ptr[m + 1] += rev_ptr[m];
-  rev.resize(rev_ptr[nelem]);
-  {
-    std::vector<int> fill(rev_ptr.begin(), rev_ptr.end() - 1);
-    for (int k = 0; k < nelem; k++)
-      for (int i = mptr[k]; i < mptr[k + 1]; i++) rev[fill[mdep[i]]++] = k;
-  }
-  for (int j = 0; j < nface; j++) {
-    items1.push_back(code(0, j));
-    for (int m : after_face[j]) {
-      items1.push_back(code(1, m));
-      for (int i = rev_ptr[m]; i < rev_ptr[m + 1]; i++)
-        if (--pending[rev[i]] == 0) items1.push_back(code(2, rev[i]));
-    }
-  }
-  if ((int)items0.size() != nface + nelem || (int)items1.size() != nface + 2 * nelem)
-    return fail(DG_BAD_MESH, "pipelined stage: incomplete work list");
-  // every item after the items it waits for (the waits then always end)
-  for (int l = 0; l < 2; l++) {
-    const std::vector<int> &it = l ? items1 : items0;
-    std::vector<int> pos(3 * (size_t)std::max(nface, nelem), -1);
-    for (size_t i = 0; i < it.size(); i++)
-      pos[(size_t)(it[i] >> 29) * std::max(nface, nelem) + (it[i] & 0x1FFFFFFF)] = (int)i;
-    auto at = [&](int type, int tile) { return pos[(size_t)type * std::max(nface, nelem) + tile]; };
-    for (int k = 0; k < nelem; k++) {
-      const int pe = at(2, k), pm = at(1, k);
-      for (int i = fptr[k]; i < fptr[k + 1]; i++)
-        if (at(0, fdep[i]) >= (l ? pm : pe)) return fail(DG_BAD_MESH, "pipelined stage: order");
-      if (l)
-        for (int i = mptr[k]; i < mptr[k + 1]; i++)
-          if (at(1, mdep[i]) >= pe) return fail(DG_BAD_MESH, "pipelined stage: order");
-    }
-  }
-  int *d_items0, *d_items1, *d_fptr, *d_fdep, *d_mptr, *d_mdep;
-  dg_status st;
-  if ((st = upload(s, &d_items0, items0)) != DG_OK) return st;
-  if ((st = upload(s, &d_items1, items1)) != DG_OK) return st;
-  if ((st = upload(s, &d_fptr, fptr)) != DG_OK) return st;
-  if ((st = upload(s, &d_fdep, fdep)) != DG_OK) return st;
-  if ((st = upload(s, &d_mptr, mptr)) != DG_OK) return st;
-  if ((st = upload(s, &d_mdep, mdep)) != DG_OK) return st;
-  if ((st = dalloc(s, &s->pipe_work, (size_t)2 + nface + nelem)) != DG_OK) return st;
-  CK(cudaMemset(s->pipe_work, 0, sizeof(int) * ((size_t)2 + nface + nelem)));
-  for (int l = 0; l < 2; l++) {
-    dg::PipeArgs &pa = s->ctx.pipe[l];
-    pa.items = l ? d_items1 : d_items0;
-    pa.nitems = l ? (int)items1.size() : (int)items0.size();
-    pa.nface = nface;
-    pa.nelem = nelem;
-    pa.work = s->pipe_work;
-    pa.fdep_ptr = d_fptr;
-    pa.fdep = d_fdep;
-    pa.mdep_ptr = d_mptr;
-    pa.mdep = d_mdep;
-    pa.lim = l;
-  }
-  return DG_OK;
-}
-
 // (re)builds the tensor-core tables from the current basis tables and
 // points the fused element stage at them (or back at the FP64 kernel)
 dg_status oz_refresh(dg_solver *s) {
@@ -424,10 +300,7 @@ dg_status oz_refresh(dg_solver *s) {
   if (!s->oz) {
     dg_status st = dalloc(s, reinterpret_cast<char **>(&s->oz), img.size());
     if (st != DG_OK) return st;
-    CK(dg::oz_prepare_euler(s->p, &s->pipe_per_sm));
-    int nsm = 0;
-    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, s->device));
-    for (auto &pa : s->ctx.pipe) pa.grid = s->pipe_per_sm * nsm;
+    CK(dg::oz_prepare_euler(s->p));
   }
   CK(cudaMemcpy(s->oz, img.data(), img.size(), cudaMemcpyHostToDevice));
   if (s->tensor) s->ctx.oz = s->oz;
@@ -501,7 +374,6 @@ dg_status run_steps(dg_solver *s, int nsteps, int scheme, double fixed_dt, doubl
   h.endtime = endtime;
   dg_status st = set_scalar(s, 0, &h, sizeof h);
   if (st != DG_OK) return st;
-  if (s->pipe_work) CK(cudaMemsetAsync(s->pipe_work + 1, 0, sizeof(int), s->st));
   const bool resume = scheme == DG_SSP_RK3 && s->tr_valid;
   s->tr_valid = false;
   if (!resume) {
@@ -550,14 +422,6 @@ dg_status run_steps(dg_solver *s, int nsteps, int scheme, double fixed_dt, doubl
   }
   st = sync_check(s);
   if (st != DG_OK) return st;
-  if (s->pipe_work) {
-    int perr = 0;
-    CK(cudaMemcpy(&perr, s->pipe_work + 1, sizeof(int), cudaMemcpyDeviceToHost));
-    if (perr) {
-      s->tr_valid = false;
-      return fail(DG_TIMEOUT, "pipelined stage: a wait for another block's work ran out");
-    }
-  }
   *t = h.t;
   if (taken) *taken = (int)h.steps;
   if (h.status == 4) return fail(DG_NAN, "time step is NaN or not positive (non-finite state?)");
@@ -779,9 +643,6 @@ extern "C" dg_status dg_solver_create(const dg_mesh *mesh, dg_equation eq, int p
   c.Fs = s->Fs;
   c.M = s->M;
   c.ds = s->ds;
-  if (s->ops->stage_pipe && p >= 1 && p <= 4) {
-    if ((st = pipe_build(s, esd, nbr)) != DG_OK) return bail(st);
-  }
   dg_status ozs = oz_refresh(s);
   if (ozs != DG_OK) return bail(ozs);
   *out = s;
@@ -2236,23 +2097,6 @@ extern "C" dg_status dg_set_tensor_contractions(dg_solver *s, int on) {
   s->tensor = on != 0;
   s->ctx.oz = s->tensor ? s->oz : nullptr;
   drop_graphs(s);
-  return DG_OK;
-}
-
-// one persistent launch per SSP-RK3 stage instead of face + means + element
-// launches (tensor-core element stage only; the same bits either way)
-extern "C" dg_status dg_set_pipelined_stage(dg_solver *s, int on) {
-  if (!s) return fail(DG_BAD_ARG, "null solver");
-  if (on && !s->pipe_work)
-    return fail(DG_UNSUPPORTED, "the pipelined stage is for the tensor-core Euler path, p = 1..4");
-  s->pipelined = on != 0;
-  drop_graphs(s);
-  return DG_OK;
-}
-
-extern "C" dg_status dg_get_pipelined_stage(dg_solver *s, int *on) {
-  if (!s || !on) return fail(DG_BAD_ARG, "null argument");
-  *on = (s->pipelined && s->pipe_work && s->ctx.oz) ? 1 : 0;
   return DG_OK;
 }
 

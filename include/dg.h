@@ -239,17 +239,6 @@ dg_status dg_set_tensor_contractions(dg_solver *s, int on);
  * PROJ x 3, TRACE) */
 dg_status dg_oz_table_image(int p, void *out, size_t bytes, double *dense);
 dg_status dg_get_tensor_contractions(dg_solver *s, int *on);
-/* With the tensor-core element stage, one SSP-RK3 stage can run as one
- * persistent launch (on by default): its blocks take face tiles (128 sides),
- * cell-mean tiles and element tiles (64 elements) from one work list, in an
- * order where each tile needs only tiles before it, so faces and element
- * work share the SMs.  The results are bit for bit those of the separate
- * face, means and element launches.  DG_UNSUPPORTED where there is no
- * tensor-core element stage.  A wait for another block's tile that runs out
- * (about a second) ends the step with DG_TIMEOUT.  No reference
- * counterpart. */
-dg_status dg_set_pipelined_stage(dg_solver *s, int on);
-dg_status dg_get_pipelined_stage(dg_solver *s, int *on);
 
 /* binary checkpoint / restart (no reference counterpart: the reference's
  * output is vertex values only).  The file holds the equation, order,
@@ -351,8 +340,7 @@ void dg_adjoint_destroy(dg_adjoint *a);
  * of replaying a CUDA graph. */
 dg_status dg_profile_enable(dg_solver *s, int on);
 /* names: "trace", "face", "element", "limit", "cfl", "rk", "means" (the
- * fused limiter's cell means), "stage" (a pipelined stage); fills launches
- * and the
+ * fused limiter's cell means); fills launches and the
  * summed milliseconds since the last reset */
 dg_status dg_profile_get(dg_solver *s, const char *kernel, long long *launches, double *ms);
 dg_status dg_profile_reset(dg_solver *s);

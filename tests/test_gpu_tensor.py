@@ -201,32 +201,3 @@ def test_state_round_trip_through_the_host_is_invisible(dglib):
     c.set_state(x)
     assert b.step(3, dg.SSP_RK3, tb) == c.step(3, dg.SSP_RK3, tb)
     assert np.array_equal(b.get_state(), c.get_state())
-
-
-@pytest.mark.parametrize("limiter", [0, 1])
-@pytest.mark.parametrize("p", [1, 2, 3, 4])
-def test_pipelined_stage_equals_separate_launches(dglib, p, limiter):
-    """One persistent launch per stage (face, means and element tiles from
-    one work list) gives the bits of the separate face, means and element
-    launches, with and without the limiter."""
-    dg = dglib
-    mesh = dg.Mesh.square(40, 40, jitter=0.1, seed=3, bc=(-4, -4, -4, -4))
-    kw = dict(problem="euler_riemann4", limiter=limiter, cfl=0.2)
-    a, b = dg.Solver(mesh, dg.EULER, p, **kw), dg.Solver(mesh, dg.EULER, p, **kw)
-    for s in (a, b):
-        s.tensor_contractions = True
-        s.init_conditions()
-    assert a.pipelined_stage
-    b.pipelined_stage = False
-    assert not b.pipelined_stage
-    ta, tb = a.step(12, dg.SSP_RK3, 0.0), b.step(12, dg.SSP_RK3, 0.0)
-    assert ta == tb and np.array_equal(a.get_state(), b.get_state())
-
-
-def test_pipelined_stage_unsupported_without_tensor_path(dglib):
-    dg = dglib
-    mesh = dg.Mesh.square(6, 6, jitter=0.1, seed=1)
-    s = dg.Solver(mesh, dg.SHALLOW_WATER, 2, problem="sw_hump", prm=(1.0, 0.1, 0.1, 0.5, 0.5))
-    assert not s.pipelined_stage
-    with pytest.raises(dg.DGError):
-        s.pipelined_stage = True
