@@ -178,7 +178,7 @@ __device__ __forceinline__ void face_body(const Tab<P> &tab, const EqP &q, const
 #pragma unroll
       for (int n = 0; n < N; n++) {
         Fn[n] *= sc;
-        if (FS) fs[n] += Fn[n];
+        if (FS) fs[n] = j == 0 ? Fn[n] : fs[n] + Fn[n];
       }
       store_vars<N>(F + j * N, Fn);
     }
@@ -208,7 +208,7 @@ __device__ __forceinline__ void face_body(const Tab<P> &tab, const EqP &q, const
 #pragma unroll
       for (int n = 0; n < N; n++) {
         Fn[n] *= sc;
-        if (FS) fs[n] += Fn[n];
+        if (FS) fs[n] = j == 0 ? Fn[n] : fs[n] + Fn[n];
       }
       store_vars<N>(F + j * N, Fn);
     }
@@ -468,7 +468,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_means(const __grid_constant__ Tab
 #pragma unroll
   for (int n = 0; n < N; n++) {
     const size_t o = (size_t)(n * NP) * Kp + e;
-    double v = fma(sc, sum[n] * e0, a.cb * a.us[o]);
+    double v = fma(sc, sum[n] * e0, a.cb == 1.0 ? a.us[o] : a.cb * a.us[o]);
     if (a.ca != 0.0) v = fma(a.ca, a.un[o], v);
     M[(size_t)n * Kp + e] = v;
   }
