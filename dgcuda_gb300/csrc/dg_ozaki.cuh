@@ -407,23 +407,11 @@ __device__ __forceinline__ void limit_epilogue(const Tab<P> &tab, const ElemArgs
     // basis function 0 is constant: c0 phi_0 is one product for every point
     const double a0 = c0 * e0;
     const bool flat = al == 0.0 && a0 != 0.0;
-    // alpha = 0 on a zero mean (gas at rest along an axis): a0, c1 E_1 and
-    // c2 E_2 are all signed zeros, and a0 + c1 E_1 + c2 E_2 rounded to
-    // nearest is -0 exactly when all three are -0 -- the FMA chain's result,
-    // found on the integer pipe from the signs
-    const long long ka0 = __double_as_longlong(a0), kc1 = __double_as_longlong(c1),
-                    kc2 = __double_as_longlong(c2);
-    const bool zeros = al == 0.0 && !flat &&
-                       ((unsigned long long)(ka0 | kc1 | kc2) << 1) == 0ull;
 #pragma unroll
     for (int idx = 0; idx < NF; idx++) {
       const int f = idx / N1, j = idx % N1, pp = idx >> 2, tt = idx & 3;
       double v = a0;
-      if (zeros) {
-        v = __longlong_as_double(ka0 & (kc1 ^ __double_as_longlong(tab.E[f][j][1])) &
-                                 (kc2 ^ __double_as_longlong(tab.E[f][j][2])) &
-                                 (long long)0x8000000000000000ull);
-      } else if (!flat) {
+      if (!flat) {
         v = fma(c1, tab.E[f][j][1], v);
         v = fma(c2, tab.E[f][j][2], v);
       }
@@ -741,8 +729,7 @@ __global__ void __launch_bounds__(kOzThreads, P <= 3 ? 4 : 3) k_element_oz(const
         if (p < PM && idx < NP) {
           const size_t o = (size_t)(n * NP + idx) * Kp + ec[e];
           const double cin = (badv[e] && idx > 0) ? 0.0 : us[o];
-          // cb = 1 (the first stage): cb u_s is u_s exactly, no product
-          double v = fma(sc[e], R[p < PM ? p : 0][e], a.cb == 1.0 ? cin : a.cb * cin);
+          double v = fma(sc[e], R[p < PM ? p : 0][e], a.cb * cin);
           if (a.ca != 0.0) v = fma(a.ca, a.un[o], v);
           // LIM: mode 0 is the mean k_means stored, which the neighbours'
           // limiters read (the same value up to the rounding of its sum)
