@@ -35,6 +35,7 @@
 // mode and point instead of 6), and the limiter needs two divisions per
 // variable instead of one per edge point.
 #pragma once
+#include <algorithm>
 #include "dg_device.cuh"
 #include "dg_launch.h"
 
@@ -688,12 +689,38 @@ __device__ __forceinline__ void lambda_body(const Tab<P> &tab, const EqP &q,
   }
 }
 
+// the same maximum over a single problem, grid-stride: a few blocks per SM
+// each take the max over many elements, so one atomic per block stays cheap
+// (one per 128 elements serialises on the one word)
+constexpr int kLambdaBlocks = 1024;
 template <class Eq, int P>
 __global__ void __launch_bounds__(kBlock) k_lambda(const __grid_constant__ Tab<P> tab,
                                                    const __grid_constant__ EqP q,
                                                    const double *__restrict__ u, DevScalars *ds,
                                                    int K, int Kp) {
-  lambda_body<Eq, P>(tab, q, u, ds, K, Kp, blockIdx.x * blockDim.x + threadIdx.x);
+  constexpr int N = Eq::N, NP = Tab<P>::NP;
+  double lam = 0.0;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < K; e += gridDim.x * blockDim.x) {
+    double U[N];
+#pragma unroll
+    for (int n = 0; n < N; n++) U[n] = u[(size_t)(n * NP) * Kp + e] * tab.B[0][0];
+    double l = Eq::mean_speed(q, U);
+    if (!(l == l)) {
+      atomicExch(&ds->status, 4);
+      l = 0.0;
+    }
+    lam = fmax(lam, l);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) lam = fmax(lam, __shfl_xor_sync(0xffffffffu, lam, o));
+  __shared__ double sm[kBlock / 32];
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = lam;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = sm[0];
+    for (int w = 1; w < kBlock / 32; w++) m = fmax(m, sm[w]);
+    atomicMax(&ds->lam_bits, (unsigned long long)__double_as_longlong(m));
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1052,8 +1079,9 @@ struct Launch {
                                                                           c.m.K, c.m.Kp)));
   }
   static void lambda(const Ctx &c, const double *u) {
-    DG_DISPATCH_P((k_lambda<Eq, P><<<nblk(c.m.K), kBlock, 0, c.st>>>(tab<P>(c), *c.q, u, c.ds,
-                                                                      c.m.K, c.m.Kp)));
+    const unsigned g = std::min(nblk(c.m.K), (unsigned)kLambdaBlocks);
+    DG_DISPATCH_P((k_lambda<Eq, P><<<g, kBlock, 0, c.st>>>(tab<P>(c), *c.q, u, c.ds, c.m.K,
+                                                            c.m.Kp)));
   }
   static void init(const Ctx &c, double *u) {
     DG_DISPATCH_P((k_init<Eq, P><<<nblk(c.m.K), kBlock, 0, c.st>>>(tab<P>(c), *c.q, u,
