@@ -201,3 +201,21 @@ def test_state_round_trip_through_the_host_is_invisible(dglib):
     c.set_state(x)
     assert b.step(3, dg.SSP_RK3, tb) == c.step(3, dg.SSP_RK3, tb)
     assert np.array_equal(b.get_state(), c.get_state())
+
+
+@pytest.mark.parametrize("p", [1, 2, 4])
+def test_fused_limiter_matches_oracle(dglib, oracle_mod, p):
+    """The limiter in the tensor-core element stage's epilogue at the orders
+    the full-size test does not run on small meshes: p = 1 (no free shared-
+    memory slot: the limiter rereads modes 1 and 2 from the output), p = 2,
+    p = 4; four-quadrant Riemann problem, transmissive sides, 8 steps."""
+    dg = dglib
+    mesh = dg.Mesh.square(20, 20, jitter=0.1, seed=3, bc=(-4, -4, -4, -4))
+    s = dg.Solver(mesh, dg.EULER, p, problem="euler_riemann4", limiter=1, cfl=0.2)
+    s.tensor_contractions = True
+    s.init_conditions()
+    c0 = s.get_state()
+    t = s.step(8, dg.SSP_RK3, 0.0)
+    c, to, n = _oracle_run(dg, oracle_mod, mesh, p, (), "euler_riemann4", c0, 8, 1, 0.2)
+    assert n == 8 and abs(t - to) <= 1e-12 * to
+    assert relerr(s.get_state(), c, 4) <= 1e-10
