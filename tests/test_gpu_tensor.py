@@ -219,3 +219,25 @@ def test_fused_limiter_matches_oracle(dglib, oracle_mod, p):
     c, to, n = _oracle_run(dg, oracle_mod, mesh, p, (), "euler_riemann4", c0, 8, 1, 0.2)
     assert n == 8 and abs(t - to) <= 1e-12 * to
     assert relerr(s.get_state(), c, 4) <= 1e-10
+
+
+@pytest.mark.parametrize("n", [1, 3])
+def test_tensor_path_on_tiny_meshes(dglib, oracle_mod, n):
+    """K = 2 and K = 18 (one partial tile of the 64-element blocks, lanes
+    past the last element), slip walls, p = 3, limiter on: against the
+    oracle."""
+    dg = dglib
+    mesh = dg.Mesh.square(n, n, jitter=0.0, seed=1, bc=(-1, -1, -1, -1))
+    assert mesh.K == 2 * n * n
+    s = dg.Solver(mesh, dg.EULER, 3, problem="euler_riemann4", limiter=1, cfl=0.2)
+    assert s.tensor_contractions
+    s.init_conditions()
+    c0 = s.get_state()
+    t = s.step(5, dg.SSP_RK3, 0.0)
+    c, to, nst = _oracle_run(dg, oracle_mod, mesh, 3, (), "euler_riemann4", c0, 5, 1, 0.2)
+    assert nst == 5 and abs(t - to) <= 1e-12 * to
+    assert relerr(s.get_state(), c, 4) <= 1e-10
+    r = s.eval_rhs(s.get_state(), t)
+    o = oracle_mod.Oracle.from_mesh(mesh, dg.EULER, 3, oracle_mod.prm_vec(gamma=1.4),
+                                    dg.PROBLEMS["euler_riemann4"])
+    assert relerr(r, o.rhs(s.get_state(), t), 4) <= 1e-12
