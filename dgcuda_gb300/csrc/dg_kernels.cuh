@@ -291,6 +291,12 @@ __device__ __forceinline__ bool volume(const Tab<P> &tab, const EqP &q,
   return ok;
 }
 
+template <class Eq, int P>
+__device__ __forceinline__ void limit_tr_body(const Tab<P> &tab, const EqP &q, double *u,
+                                              double *__restrict__ T,
+                                              const int *__restrict__ nbr, int Kp, int e,
+                                              const double *mean, size_t mstride);
+
 // arguments of one element-kernel launch on one problem
 struct ElemArgs {
   double *us;               // stage input (flattened in place if needed)
@@ -312,7 +318,10 @@ struct ElemArgs {
 // TR: also write the edge traces of `out` into T (what k_trace would compute
 // from it at the start of the next stage, bit for bit) and, when `check` is
 // set, flatten an element whose new traces are non-physical
-template <class Eq, int P, bool TR>
+// LIM (with TR): the limiter in the epilogue -- mode 0 of the output is the
+// stored mean a.M (k_means), and limit_tr_body runs on the new modes and
+// traces with the neighbours' means from a.M
+template <class Eq, int P, bool TR, bool LIM = false>
 __device__ __forceinline__ void element_body(const Tab<P> &tab, const EqP &q, const ElemArgs &a,
                                              int e) {
   constexpr int N = Eq::N, NP = Tab<P>::NP, N1 = Tab<P>::N1;
@@ -388,6 +397,7 @@ __device__ __forceinline__ void element_body(const Tab<P> &tab, const EqP &q, co
       const size_t o = (size_t)(n * NP + i) * Kp + e;
       double v = fma(s, acc[n][i], a.cb * c[n][i]);
       if (a.ca != 0.0) v = fma(a.ca, a.un[o], v);
+      if (LIM && i == 0) v = a.M[(size_t)n * Kp + e];
       out[o] = v;
       if (TR) acc[n][i] = v;
     }
@@ -410,7 +420,7 @@ __device__ __forceinline__ void element_body(const Tab<P> &tab, const EqP &q, co
 #pragma unroll
         for (int n = 0; n < N; n++) Te[(f * N1 + j) * N + n] = U[n];
       }
-    if (a.check && bad) {
+    if (!LIM && a.check && bad) {
 #pragma unroll
       for (int n = 0; n < N; n++) {
 #pragma unroll
@@ -421,15 +431,16 @@ __device__ __forceinline__ void element_body(const Tab<P> &tab, const EqP &q, co
           for (int j = 0; j < N1; j++) Te[(f * N1 + j) * N + n] = acc[n][0] * tab.E[f][j][0];
       }
     }
+    if constexpr (LIM) limit_tr_body<Eq, P>(tab, q, out, a.T, a.nbr, Kp, e, a.M, (size_t)Kp);
   }
 }
 
-template <class Eq, int P, bool TR>
+template <class Eq, int P, bool TR, bool LIM = false>
 __global__ void __launch_bounds__(kMaxBlock) k_element(const __grid_constant__ Tab<P> tab,
                                                        const __grid_constant__ EqP q,
                                                        const __grid_constant__ ElemArgs a) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e < a.K) element_body<Eq, P, TR>(tab, q, a, e);
+  if (e < a.K) element_body<Eq, P, TR, LIM>(tab, q, a, e);
 }
 
 // ---------------------------------------------------------------------------
@@ -443,13 +454,10 @@ __global__ void __launch_bounds__(kMaxBlock) k_element(const __grid_constant__ T
 // epilogue's roundings; the element stage writes these M as the output's
 // mode 0, so the limiter's neighbour bounds see exactly the stored means.
 template <class Eq, int P>
-__global__ void __launch_bounds__(kMaxBlock) k_means(const __grid_constant__ Tab<P> tab,
-                                                     const __grid_constant__ ElemArgs a,
-                                                     const double *__restrict__ Fs,
-                                                     double *__restrict__ M) {
+__device__ __forceinline__ void means_body(const Tab<P> &tab, const ElemArgs &a,
+                                           const double *__restrict__ Fs, double *__restrict__ M,
+                                           int e) {
   constexpr int N = Eq::N, NP = Tab<P>::NP;
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= a.K) return;
   const size_t Kp = a.Kp;
   double sum[N];
 #pragma unroll
@@ -473,6 +481,15 @@ __global__ void __launch_bounds__(kMaxBlock) k_means(const __grid_constant__ Tab
     if (a.ca != 0.0) v = fma(a.ca, a.un[o], v);
     M[(size_t)n * Kp + e] = v;
   }
+}
+
+template <class Eq, int P>
+__global__ void __launch_bounds__(kMaxBlock) k_means(const __grid_constant__ Tab<P> tab,
+                                                     const __grid_constant__ ElemArgs a,
+                                                     const double *__restrict__ Fs,
+                                                     double *__restrict__ M) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < a.K) means_body<Eq, P>(tab, a, Fs, M, e);
 }
 
 // ---------------------------------------------------------------------------
@@ -560,10 +577,15 @@ __global__ void __launch_bounds__(kMaxBlock) k_limit(const __grid_constant__ Tab
 // limited modes, then the positivity rule of k_trace is applied to the final
 // traces.  T ends up holding exactly what k_trace would compute from the
 // limited state.
+// mean: the cell means (mode-0 coefficients) of variable n of element x are
+// mean[n * mstride + x]: the state's own rows (mean = u, mstride = NP Kp), or
+// the means k_means stored before the element stage wrote u (mean = M,
+// mstride = Kp), when the neighbours' rows may not be written yet
 template <class Eq, int P>
 __device__ __forceinline__ void limit_tr_body(const Tab<P> &tab, const EqP &q, double *u,
                                               double *__restrict__ T,
-                                              const int *__restrict__ nbr, int Kp, int e) {
+                                              const int *__restrict__ nbr, int Kp, int e,
+                                              const double *mean, size_t mstride) {
   constexpr int N = Eq::N, NP = Tab<P>::NP, N1 = Tab<P>::N1;
   const int nb0 = nbr[e], nb1 = nbr[(size_t)Kp + e], nb2 = nbr[2 * (size_t)Kp + e];
   const double phi0 = tab.B[0][0];
@@ -573,12 +595,13 @@ __device__ __forceinline__ void limit_tr_body(const Tab<P> &tab, const EqP &q, d
 #pragma unroll
   for (int n = 0; n < N; n++) {
     double *row = u + (size_t)(n * NP) * Kp;
-    c0[n] = row[e];
+    const double *mn = mean + (size_t)n * mstride;
+    c0[n] = mn[e];
     // products reused as addends are rounded explicitly (__dmul_rn is never
     // fused into an FMA), so every kernel instance rounds them the same way
     const double Uc = __dmul_rn(c0[n], phi0);
     double Umin, Umax;
-    mean_bounds(c0[n], row[nb0], row[nb1], row[nb2], phi0, Umin, Umax);
+    mean_bounds(c0[n], mn[nb0], mn[nb1], mn[nb2], phi0, Umin, Umax);
     // max_k (T_k - Uc) = max_k T_k - Uc exactly (rounding is monotonic), so
     // the extremes of the edge values are found first, on the integer pipe
     // (order_key), and each is subtracted once
@@ -655,7 +678,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_limit_tr(const __grid_constant__ 
                                                         const int *__restrict__ nbr, int K,
                                                         int Kp) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e < K) limit_tr_body<Eq, P>(tab, q, u, T, nbr, Kp, e);
+  if (e < K) limit_tr_body<Eq, P>(tab, q, u, T, nbr, Kp, e, u, (size_t)Tab<P>::NP * Kp);
 }
 
 // ---------------------------------------------------------------------------
@@ -864,7 +887,7 @@ __device__ __forceinline__ ElemArgs batch_elem_args(const BatchProb &pr, int sta
   a.bathy = pr.bathy;
   a.vtx = pr.vtx;
   a.T = pr.T;
-  a.M = nullptr;
+  a.M = pr.M;
   a.nbr = pr.nbr;
   a.ca = stage == 0 ? 0.0 : stage == 1 ? 0.75 : 1.0 / 3.0;
   a.cb = stage == 0 ? 1.0 : stage == 1 ? 0.25 : 2.0 / 3.0;
@@ -879,7 +902,7 @@ __device__ __forceinline__ ElemArgs batch_elem_args(const BatchProb &pr, int sta
 // gridDim.x) of the problems of one order P and one mesh-size group (the
 // block map lists the problems by group): one launch per group, each at its
 // own register count and block size
-template <class Eq, int P>
+template <class Eq, int P, bool LIM = false>
 __global__ void __launch_bounds__(kMaxBlock)
     k_element_batch_p(const __grid_constant__ Tab<P> tab, const BatchProb *__restrict__ probs,
                       const int *__restrict__ blk2prob, const int *__restrict__ blk0, int b_lo,
@@ -890,10 +913,28 @@ __global__ void __launch_bounds__(kMaxBlock)
   const int e = (b - blk0[pi]) * blockDim.x + threadIdx.x;
   if (e >= pr.K) return;
   const ElemArgs a = batch_elem_args(pr, stage, check);
-  element_body<Eq, P, true>(tab, pr.q, a, e);
+  element_body<Eq, P, true, LIM>(tab, pr.q, a, e);
 }
 
+// the next stage output's cell means of every member (k_means), over the
+// element blocks of the shared block size
 template <class Eq>
+__global__ void __launch_bounds__(kMaxBlock)
+    k_means_batch(const __grid_constant__ BatchTabs tb, const BatchProb *__restrict__ probs,
+                  const int *__restrict__ blk2prob, const int *__restrict__ blk0, int stage) {
+  const int pi = blk2prob[blockIdx.x];
+  const BatchProb &pr = probs[pi];
+  const int e = (blockIdx.x - blk0[pi]) * blockDim.x + threadIdx.x;
+  if (e >= pr.K) return;
+  const ElemArgs a = batch_elem_args(pr, stage, 0);
+  switch (pr.p) {
+    case 1: means_body<Eq, 1>(tb.t1, a, pr.Fs, pr.M, e); break;
+    case 2: means_body<Eq, 2>(tb.t2, a, pr.Fs, pr.M, e); break;
+    case 3: means_body<Eq, 3>(tb.t3, a, pr.Fs, pr.M, e); break;
+  }
+}
+
+template <class Eq, bool FS = false>
 __global__ void __launch_bounds__(kMaxBlock)
     k_face_batch(const __grid_constant__ BatchTabs tb, const BatchProb *__restrict__ probs,
                  const int *__restrict__ blk2prob, const int *__restrict__ blk0, double tcoef) {
@@ -908,7 +949,7 @@ __global__ void __launch_bounds__(kMaxBlock)
   a.bxy = pr.bxy;
   a.vtx = pr.vtx;
   a.Fh = pr.Fh;
-  a.Fs = nullptr;
+  a.Fs = pr.Fs;
   a.tptr = &pr.ds->t;
   a.dtp = &pr.ds->dt;
   a.tcoef = tcoef;
@@ -916,9 +957,9 @@ __global__ void __launch_bounds__(kMaxBlock)
   a.Sb = pr.Sb;
   a.Kp = pr.Kp;
   switch (pr.p) {
-    case 1: face_body<Eq, 1>(tb.t1, pr.q, a, s); break;
-    case 2: face_body<Eq, 2>(tb.t2, pr.q, a, s); break;
-    case 3: face_body<Eq, 3>(tb.t3, pr.q, a, s); break;
+    case 1: face_body<Eq, 1, FS>(tb.t1, pr.q, a, s); break;
+    case 2: face_body<Eq, 2, FS>(tb.t2, pr.q, a, s); break;
+    case 3: face_body<Eq, 3, FS>(tb.t3, pr.q, a, s); break;
   }
 }
 
@@ -932,9 +973,9 @@ __global__ void __launch_bounds__(kMaxBlock)
   if (e >= pr.K) return;
   double *u = stage == 2 ? pr.U : pr.W;
   switch (pr.p) {
-    case 1: limit_tr_body<Eq, 1>(tb.t1, pr.q, u, pr.T, pr.nbr, pr.Kp, e); break;
-    case 2: limit_tr_body<Eq, 2>(tb.t2, pr.q, u, pr.T, pr.nbr, pr.Kp, e); break;
-    case 3: limit_tr_body<Eq, 3>(tb.t3, pr.q, u, pr.T, pr.nbr, pr.Kp, e); break;
+    case 1: limit_tr_body<Eq, 1>(tb.t1, pr.q, u, pr.T, pr.nbr, pr.Kp, e, u, (size_t)Tab<1>::NP * pr.Kp); break;
+    case 2: limit_tr_body<Eq, 2>(tb.t2, pr.q, u, pr.T, pr.nbr, pr.Kp, e, u, (size_t)Tab<2>::NP * pr.Kp); break;
+    case 3: limit_tr_body<Eq, 3>(tb.t3, pr.q, u, pr.T, pr.nbr, pr.Kp, e, u, (size_t)Tab<3>::NP * pr.Kp); break;
   }
 }
 
@@ -1061,6 +1102,15 @@ struct Launch {
     DG_DISPATCH_P((k_element<Eq, P, false><<<nblk(c.m.K, c.blk), c.blk, 0, c.st>>>(tab<P>(c),
                                                                                    *c.q, a)));
   }
+  // element_tr() with the limiter in the epilogue (c.M holds the output's
+  // means from k_means)
+  static void element_lim(const Ctx &c, double *us, const double *un, double *out, double ca,
+                          double cb, double cc, const double *dtp) {
+    if (!c.m.K) return;
+    const ElemArgs a = eargs(c, us, un, out, ca, cb, cc, dtp, c.T, 0);
+    DG_DISPATCH_P((k_element<Eq, P, true, true><<<nblk(c.m.K, c.blk), c.blk, 0, c.st>>>(
+        tab<P>(c), *c.q, a)));
+  }
   static void element_tr(const Ctx &c, double *us, const double *un, double *out, double ca,
                          double cb, double cc, const double *dtp, int check) {
     if (!c.m.K) return;
@@ -1116,7 +1166,8 @@ struct Launch {
     k_face_batch<Eq><<<b.nsblk, b.blk, 0, b.st>>>(btabs(b), b.probs, b.sblk2prob, b.sblk0,
                                                    tcoef);
   }
-  static void b_element(const BatchLaunch &b, int stage) {
+  template <bool LIM>
+  static void b_element_v(const BatchLaunch &b, int stage) {
     const BatchTabs &tb = btabs(b);
     const int check = b.limiter ? 0 : 1;
     // one launch per (order, mesh-size) group, each with its own block size
@@ -1124,15 +1175,26 @@ struct Launch {
       const int lo = b.eblk_g[g], n = b.eblk_g[g + 1] - lo, p = 1 + g / 2, blk = b.blk_g[g];
       if (n <= 0) continue;
       if (p == 1)
-        k_element_batch_p<Eq, 1><<<n, blk, 0, b.st>>>(tb.t1, b.probs, b.eblk2prob, b.eblk0, lo,
-                                                        stage, check);
+        k_element_batch_p<Eq, 1, LIM><<<n, blk, 0, b.st>>>(tb.t1, b.probs, b.eblk2prob, b.eblk0,
+                                                             lo, stage, check);
       else if (p == 2)
-        k_element_batch_p<Eq, 2><<<n, blk, 0, b.st>>>(tb.t2, b.probs, b.eblk2prob, b.eblk0, lo,
-                                                        stage, check);
+        k_element_batch_p<Eq, 2, LIM><<<n, blk, 0, b.st>>>(tb.t2, b.probs, b.eblk2prob, b.eblk0,
+                                                             lo, stage, check);
       else
-        k_element_batch_p<Eq, 3><<<n, blk, 0, b.st>>>(tb.t3, b.probs, b.eblk2prob, b.eblk0, lo,
-                                                        stage, check);
+        k_element_batch_p<Eq, 3, LIM><<<n, blk, 0, b.st>>>(tb.t3, b.probs, b.eblk2prob, b.eblk0,
+                                                             lo, stage, check);
     }
+  }
+  static void b_element(const BatchLaunch &b, int stage) { b_element_v<false>(b, stage); }
+  // the fused-limiter stage (instantiated only where an equation uses it)
+  static void b_element_lim(const BatchLaunch &b, int stage) { b_element_v<true>(b, stage); }
+  static void b_face_fs(const BatchLaunch &b, double tcoef) {
+    k_face_batch<Eq, true><<<b.nsblk, b.blk, 0, b.st>>>(btabs(b), b.probs, b.sblk2prob, b.sblk0,
+                                                         tcoef);
+  }
+  static void b_means(const BatchLaunch &b, int stage) {
+    k_means_batch<Eq><<<b.nublk, b.blk, 0, b.st>>>(btabs(b), b.probs, b.ublk2prob, b.ublk0,
+                                                    stage);
   }
   static void b_limit_tr(const BatchLaunch &b, int stage) {
     k_limit_tr_batch<Eq><<<b.nublk, b.blk, 0, b.st>>>(btabs(b), b.probs, b.ublk2prob, b.ublk0,
@@ -1142,7 +1204,8 @@ struct Launch {
     k_lambda_batch<Eq><<<b.nlblk, kBlock, 0, b.st>>>(btabs(b), b.probs, b.lblk2prob, b.lblk0);
   }
   static const BatchOps &batch_ops() {
-    static const BatchOps o = {b_trace, b_face, b_element, b_limit_tr, b_lambda};
+    static const BatchOps o = {b_trace, b_face,   b_element, b_limit_tr,
+                               b_lambda, nullptr, nullptr,   nullptr};
     return o;
   }
 };

@@ -29,10 +29,14 @@ void element_tr(const Ctx &c, double *us, const double *un, double *out, double 
   oz_element(c, L::eargs(c, us, un, out, ca, cb, cc, dtp, c.T, check), false);
 }
 
-// the element stage with the limiter in its epilogue (tensor path only; M
-// holds the output's means from k_means)
+// the element stage with the limiter in its epilogue (M holds the output's
+// means from k_means): the tensor-core kernel, or the FP64 one
 void element_lim(const Ctx &c, double *us, const double *un, double *out, double ca, double cb,
                  double cc, const double *dtp) {
+  if (!c.oz || c.p < 1 || c.p > 4) {
+    L::element_lim(c, us, un, out, ca, cb, cc, dtp);
+    return;
+  }
   if (!c.m.K) return;
   oz_element(c, L::eargs(c, us, un, out, ca, cb, cc, dtp, c.T, 0), true);
 }
@@ -67,7 +71,16 @@ const Ops &ops_euler() {
   static const Ops o = make_ops();
   return o;
 }
-const BatchOps &batch_ops_euler() { return Launch<Euler>::batch_ops(); }
+const BatchOps &batch_ops_euler() {
+  static const BatchOps o = [] {
+    BatchOps b = Launch<Euler>::batch_ops();
+    b.face_fs = Launch<Euler>::b_face_fs;
+    b.means = Launch<Euler>::b_means;
+    b.element_lim = Launch<Euler>::b_element_lim;
+    return b;
+  }();
+  return o;
+}
 
 // allows the tensor-core element kernels of order p their shared memory
 // (once per device, before any capture)

@@ -75,6 +75,7 @@ struct Ctx {
 struct BatchProb {
   int p, K, Kp, S, Sb, pad;
   double *U, *W, *T, *Fh;
+  double *Fs, *M;  // per-side flux sums and output means (fused limiter; null elsewhere)
   const double *geo;
   const int *esd, *nbr;
   const int4 *side;
@@ -89,6 +90,7 @@ struct BatchLaunch {
   const void *tabs = nullptr;       // BatchTabs image (Tab<1>, Tab<2>, Tab<3>)
   BatchProb *probs = nullptr;       // device array
   int nprob = 0, blk = 128, limiter = 0;
+  int fused = 0;  // limiter in the element epilogue (face_fs, means, element_lim)
   // element blocks of the element stage: group g = 2 (p - 1) + (K >= 16384)
   // holds the members of order p on small (0) or large (1) meshes, in blocks
   // of blk_g[g] elements, the blocks [eblk_g[g], eblk_g[g + 1])
@@ -108,6 +110,11 @@ struct BatchOps {
   void (*element)(const BatchLaunch &, int stage);
   void (*limit_tr)(const BatchLaunch &, int stage);
   void (*lambda)(const BatchLaunch &);
+  // the stage with the limiter in the element epilogue, as Ops::face_fs,
+  // means and element_lim (null where an equation has none)
+  void (*face_fs)(const BatchLaunch &, double tcoef);
+  void (*means)(const BatchLaunch &, int stage);
+  void (*element_lim)(const BatchLaunch &, int stage);
 };
 
 const BatchOps &batch_ops_advection();

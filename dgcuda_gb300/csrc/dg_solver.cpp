@@ -181,14 +181,14 @@ void limit(dg_solver *s, double *u) {
 
 // a stage whose input traces are already in T (left by the previous stage);
 // it leaves the traces of `out` -- limited when the limiter is on -- in T.
-// With the limiter on and the tensor-core element stage, the limiter runs in
-// that stage's epilogue: the face kernel also sums each side's fluxes, and
+// With the limiter on (Euler), the limiter runs in the element stage's
+// epilogue: the face kernel also sums each side's fluxes, and
 // k_means turns the sums into the output's cell means, which the element
 // stage needs for its neighbours' bounds; no separate limiter pass.
 void fused_stage(dg_solver *s, double *us, const double *un, double *out, double ca, double cb,
                  double cc, double tcoef, const double *dtp) {
   const bool lim = s->prm.limiter && s->np >= 3;
-  if (lim && s->ctx.oz && s->ops->element_lim && s->ctx.M) {
+  if (lim && s->ops->element_lim && s->ctx.M) {
     run(s, K_FACE, [&] { s->ops->face_fs(s->ctx, &s->ds->t, tcoef); });
     run(s, K_MEANS, [&] { s->ops->means(s->ctx, us, un, ca, cb, cc, dtp); });
     run(s, K_ELEMENT, [&] { s->ops->element_lim(s->ctx, us, un, out, ca, cb, cc, dtp); });
@@ -1222,6 +1222,12 @@ void batch_step_seq(dg_batch *b) {
   dg::launch_batch_compute_dt(L.st, L.probs, L.nprob);
   const double tc[3] = {0.0, 1.0, 0.5};
   for (int stage = 0; stage < 3; stage++) {
+    if (L.fused) {  // the limiter in the element epilogue, as the members' own steps
+      b->ops->face_fs(L, tc[stage]);
+      b->ops->means(L, stage);
+      b->ops->element_lim(L, stage);
+      continue;
+    }
     b->ops->face(L, tc[stage]);
     b->ops->element(L, stage);
     if (L.limiter) b->ops->limit_tr(L, stage);
@@ -1326,6 +1332,8 @@ extern "C" dg_status dg_batch_create(int n, dg_solver *const *members, dg_batch 
     q.W = s->W;
     q.T = s->T;
     q.Fh = s->Fh;
+    q.Fs = s->Fs;
+    q.M = s->M;
     q.geo = s->m.geo;
     q.esd = s->m.esd;
     q.nbr = s->m.nbr;
@@ -1347,6 +1355,13 @@ extern "C" dg_status dg_batch_create(int n, dg_solver *const *members, dg_batch 
   b->bl.probs = b->probs;
   b->bl.nprob = n;
   b->bl.limiter = b->limiter;
+  // with the limiter, the members' own steps limit in the element epilogue
+  // where their equation has that stage (fused_stage): the batch does the same
+  {
+    bool all = b->limiter && b->ops->element_lim;
+    for (auto *s : b->m) all = all && s->M && s->np >= 3;
+    b->bl.fused = all ? 1 : 0;
+  }
   dg_status st = batch_build_maps(b);
   if (st != DG_OK) return bail(st);
   *out = b;
