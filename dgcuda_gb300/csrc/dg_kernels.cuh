@@ -23,9 +23,14 @@
 //   k_limit    Barth-Jespersen limiter in place (limit_c, :640-720).
 //
 // SSP-RK3 steps skip k_trace after the first stage: k_element<TR=true>
-// writes the traces of its output as it stores it, and k_limit_tr limits
-// from those traces and rebuilds the ones it changes, so T always holds what
-// k_trace would have computed from the next stage's input.
+// writes the traces of its output as it stores it, so T always holds what
+// k_trace would have computed from the next stage's input.  With the limiter
+// on, the limiter runs on those traces: for Euler in the element kernel's own
+// epilogue (k_element<TR, LIM>, or k_element_oz<LIM> on the tensor path),
+// with the neighbours' new cell means found before the element stage by
+// k_means from the per-side flux sums k_face<FS> leaves; for the other
+// equations as the pass k_limit_tr.  Either way a limited element's traces
+// are rebuilt from its limited modes.
 //
 // FP64 is the binding resource on GB300 (the FP64 pipe runs at 1/62 of the
 // FP32 rate), so the design minimises FP64 instructions: every basis value
