@@ -468,12 +468,15 @@ def main():
     except (OSError, ValueError):
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    traffic = None
+    traffic, stage_traffic = None, None
     try:
         tr = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
         key = "euler_p%d_%s" % (p, dom)
         if key in tr:
             traffic = tr[key]["dram_bytes_per_element"] * K
+        parts = ["euler_p%d_%s" % (p, k) for k in ("face", "means", "element")]
+        if all(k in tr for k in parts):
+            stage_traffic = sum(tr[k]["dram_bytes_per_element"] for k in parts) * K
     except (OSError, ValueError, KeyError):
         pass
     stage_total_ms = sum(kern[k][1] for k in ("trace", "face", "element", "limit", "means")) / (
@@ -553,6 +556,12 @@ def main():
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
                          "alg_bytes_per_element": bpe,
+                         "kernel_work": ("area values, fluxes, volume + surface projection, "
+                                         "RK combination, next-stage traces and the limiter"),
+                         "stage_ms": stage_total_ms,
+                         "stage_achieved": K * bpe / (stage_total_ms / 1e3) / 1e9,
+                         "stage_frac": K * bpe / (stage_total_ms / 1e3) / 1e9 / hbm_peak,
+                         "stage_traffic": stage_traffic,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
                          "binding": ("latency of the element stage (tensor-core contractions, "
                                      "FP64 fluxes, integer slicing)" if tensor else "fp64"),
