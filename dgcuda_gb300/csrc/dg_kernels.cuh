@@ -1175,19 +1175,30 @@ struct Launch {
   static void b_element_v(const BatchLaunch &b, int stage) {
     const BatchTabs &tb = btabs(b);
     const int check = b.limiter ? 0 : 1;
-    // one launch per (order, mesh-size) group, each with its own block size
+    // one launch per (order, mesh-size) group, each with its own block size;
+    // the groups after the first on their own streams, concurrent with it
+    bool first = true;
+    if (b.fork) cudaEventRecord(b.fork, b.st);
     for (int g = 0; g < BatchLaunch::kGroups; g++) {
       const int lo = b.eblk_g[g], n = b.eblk_g[g + 1] - lo, p = 1 + g / 2, blk = b.blk_g[g];
       if (n <= 0) continue;
+      const bool side = b.fork && !first;
+      const cudaStream_t st = side ? b.gst[g] : b.st;
+      first = false;
+      if (side) cudaStreamWaitEvent(st, b.fork, 0);
       if (p == 1)
-        k_element_batch_p<Eq, 1, LIM><<<n, blk, 0, b.st>>>(tb.t1, b.probs, b.eblk2prob, b.eblk0,
-                                                             lo, stage, check);
+        k_element_batch_p<Eq, 1, LIM><<<n, blk, 0, st>>>(tb.t1, b.probs, b.eblk2prob, b.eblk0,
+                                                           lo, stage, check);
       else if (p == 2)
-        k_element_batch_p<Eq, 2, LIM><<<n, blk, 0, b.st>>>(tb.t2, b.probs, b.eblk2prob, b.eblk0,
-                                                             lo, stage, check);
+        k_element_batch_p<Eq, 2, LIM><<<n, blk, 0, st>>>(tb.t2, b.probs, b.eblk2prob, b.eblk0,
+                                                           lo, stage, check);
       else
-        k_element_batch_p<Eq, 3, LIM><<<n, blk, 0, b.st>>>(tb.t3, b.probs, b.eblk2prob, b.eblk0,
-                                                             lo, stage, check);
+        k_element_batch_p<Eq, 3, LIM><<<n, blk, 0, st>>>(tb.t3, b.probs, b.eblk2prob, b.eblk0,
+                                                           lo, stage, check);
+      if (side) {
+        cudaEventRecord(b.join[g], st);
+        cudaStreamWaitEvent(b.st, b.join[g], 0);
+      }
     }
   }
   static void b_element(const BatchLaunch &b, int stage) { b_element_v<false>(b, stage); }

@@ -102,6 +102,12 @@ struct BatchLaunch {
   static constexpr int kGroups = 6;
   int eblk_g[kGroups + 1] = {0, 0, 0, 0, 0, 0, 0};
   int blk_g[kGroups] = {128, 128, 128, 128, 128, 128};
+  // the groups' element launches are independent: the first non-empty group
+  // runs on st, every other one on gst[g], forked from st by `fork` and
+  // joined back by join[g], so a captured step holds them as parallel
+  // branches (fork null: all on st)
+  cudaStream_t gst[kGroups] = {};
+  cudaEvent_t fork = nullptr, join[kGroups] = {};
 };
 
 struct BatchOps {

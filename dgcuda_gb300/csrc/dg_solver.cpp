@@ -1351,6 +1351,13 @@ extern "C" dg_status dg_batch_create(int n, dg_solver *const *members, dg_batch 
       cudaSuccess)
     return bail(fail(DG_CUDA_ERROR, "cudaMemcpy"));
   b->bl.st = b->st;
+  for (int g = 0; g < dg::BatchLaunch::kGroups; g++) {
+    if (cudaStreamCreateWithFlags(&b->bl.gst[g], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->bl.join[g], cudaEventDisableTiming) != cudaSuccess)
+      return bail(fail(DG_CUDA_ERROR, "batch group streams"));
+  }
+  if (cudaEventCreateWithFlags(&b->bl.fork, cudaEventDisableTiming) != cudaSuccess)
+    return bail(fail(DG_CUDA_ERROR, "batch group streams"));
   b->bl.tabs = b->tabs.data();
   b->bl.probs = b->probs;
   b->bl.nprob = n;
@@ -1440,6 +1447,11 @@ extern "C" void dg_batch_destroy(dg_batch *b) {
   if (b->graph) cudaGraphExecDestroy(b->graph);
   if (b->maps) cudaFree(b->maps);
   if (b->probs) cudaFree(b->probs);
+  for (int g = 0; g < dg::BatchLaunch::kGroups; g++) {
+    if (b->bl.gst[g]) cudaStreamDestroy(b->bl.gst[g]);
+    if (b->bl.join[g]) cudaEventDestroy(b->bl.join[g]);
+  }
+  if (b->bl.fork) cudaEventDestroy(b->bl.fork);
   if (b->st) cudaStreamDestroy(b->st);
   delete b;
 }
