@@ -330,6 +330,16 @@ __device__ __forceinline__ void limit_epilogue(const Tab<P> &tab, const ElemArgs
   const int t = lane & 3, q0 = lane & ~3;
   const size_t Kp = a.Kp;
   const double phi0 = tab.B[0][0], e0 = tab.E[0][0][0];
+  // the means of this lane's variable in both elements and their neighbours,
+  // loaded first so that their latency passes under the extremes below
+  const double *Mn = a.M + (size_t)(t < N ? t : 0) * Kp;
+  double cm[2], nm[2][3];
+#pragma unroll
+  for (int e = 0; e < 2; e++) {
+    cm[e] = Mn[ec[e]];
+#pragma unroll
+    for (int f = 0; f < 3; f++) nm[e][f] = Mn[a.nbr[(size_t)f * Kp + ec[e]]];
+  }
   // ---- extremes: per lane and variable, then reduce-scatter over the quad
   long long kx[2][4], kn[2][4];
 #pragma unroll
@@ -374,16 +384,14 @@ __device__ __forceinline__ void limit_epilogue(const Tab<P> &tab, const ElemArgs
   }
   if (t >= N) return;  // (no lane is idle at N = 4)
   const int n = t;
-  const double *Mn = a.M + (size_t)n * Kp;
   double *outn = a.out + (size_t)(n * NP) * Kp;
 #pragma unroll
   for (int e = 0; e < 2; e++) {
-    const double c0 = Mn[ec[e]];
-    const int nb0 = a.nbr[ec[e]], nb1 = a.nbr[Kp + ec[e]], nb2 = a.nbr[2 * Kp + ec[e]];
+    const double c0 = cm[e];
     // products reused as addends are rounded explicitly, as in limit_tr_body
     const double Uc = __dmul_rn(c0, phi0);
     double Umin, Umax;
-    mean_bounds(c0, Mn[nb0], Mn[nb1], Mn[nb2], phi0, Umin, Umax);
+    mean_bounds(c0, nm[e][0], nm[e][1], nm[e][2], phi0, Umin, Umax);
     const double up = fmax(0.0, from_order_key(mx[e]) - Uc);
     const double dn = fmax(0.0, Uc - from_order_key(mn[e]));
     double al = 1.0;
@@ -804,10 +812,11 @@ __global__ void __launch_bounds__(kOzThreads, P <= 3 ? 4 : 3) k_element_oz(const
       const int idx = p * 4 + t;
       if (idx >= NF) continue;
       const int f = idx / N1, j = idx % N1;
+      double v[N];
 #pragma unroll
       for (int n = 0; n < N; n++)
-        Te[idx * N + n] =
-            badt[e] ? c0[n] * tab.E[f][j][0] : gh[gh_slot<N>(n, p >> 1, e, p & 1) + lane];
+        v[n] = badt[e] ? c0[n] * tab.E[f][j][0] : gh[gh_slot<N>(n, p >> 1, e, p & 1) + lane];
+      store_vars<N>(Te + idx * N, v);  // 128-bit stores
     }
   }
   if (badt[0] || badt[1]) {
@@ -897,8 +906,10 @@ __global__ void __launch_bounds__(kOzThreads) k_trace_oz(const __grid_constant__
       const int idx = p * 4 + t;
       if (idx >= NF) continue;
       const int f = idx / N1, j = idx % N1;
+      double v[N];
 #pragma unroll
-      for (int n = 0; n < N; n++) Te[idx * N + n] = bad[e] ? c0[n] * tab.E[f][j][0] : Tv[n][p][e];
+      for (int n = 0; n < N; n++) v[n] = bad[e] ? c0[n] * tab.E[f][j][0] : Tv[n][p][e];
+      store_vars<N>(Te + idx * N, v);
     }
   }
   if (bad[0] || bad[1]) {
