@@ -462,10 +462,13 @@ struct Euler {  // euler/euler.cu
     F[3] = fma(lam, UL[3] - UR[3], fma(UL[3] + pl, snl, (UR[3] + pr) * snr));
   }
   DG_HD static double mean_speed(const EqP &q, const double *U) {  // euler.cu:248-277
+    // 1/rho and the square roots within 1 ulp of IEEE division and sqrt
+    // (rcp, sqrt_pos): the wave speed is the CFL step's to 1e-15
+    const double ir = rcp(U[0]);
     const double m2 = fma(U[1], U[1], U[2] * U[2]);
-    double p = (q.gamma - 1.) * (U[3] - m2 / 2. / U[0]);
-    double c = sqrt(q.gamma * p / U[0]);
-    double s = sqrt(m2) / U[0];
+    const double p = (q.gamma - 1.) * fma(-0.5 * m2, ir, U[3]);
+    const double c = sqrt_pos(q.gamma * p * ir);
+    const double s = sqrt_pos(m2) * ir;
     return s > 0 ? s + c : -s + c;
   }
   DG_HD static void reflect(const EqP &q, const double *UL, double *UR, double x, double y,
@@ -526,8 +529,9 @@ struct ShallowWater {  // shallowwater/shallowwater.cu (g is a parameter here)
     F[2] = fma(lam, UL[2] - UR[2], fma(UL[2], snl, fma(UR[2], snr, P * ny)));
   }
   DG_HD static double mean_speed(const EqP &q, const double *U) {  // shallowwater.cu:196-224
-    double c = sqrt(U[0] * q.g);
-    double s = sqrt(fma(U[1], U[1], U[2] * U[2])) / U[0];
+    // as Euler's: rcp and sqrt_pos within 1 ulp of IEEE division and sqrt
+    const double c = sqrt_pos(U[0] * q.g);
+    const double s = sqrt_pos(fma(U[1], U[1], U[2] * U[2])) * rcp(U[0]);
     return s > 0 ? s + c : -s + c;
   }
   DG_HD static void reflect(const EqP &, const double *UL, double *UR, double, double, double nx,
