@@ -498,19 +498,23 @@ def main():
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         te = t
+        marks = [t0]
         for _ in range(args.e2e_steps):
             s.set_state(h)
             te = s.step(1, dg.SSP_RK3, te)
             s.get_state(out=h)
-        el = time.perf_counter() - t0
+            marks.append(time.perf_counter())
+        el = marks[-1] - t0
+        per = sorted(1e3 * (b - a) for a, b in zip(marks, marks[1:]))
         e2e_value, el = reduce_replicas(K * N * npm * 3 * args.e2e_steps, el,
                                         dist if world > 1 else None)
         nb = N * npm * K * 8
         e2e = {"value": e2e_value, "unit": UNIT,
                "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb,
                "steps": args.e2e_steps,
+               "ms_per_step": {"min": per[0], "median": per[len(per) // 2], "max": per[-1]},
                "note": "per step: dg_set_state from pinned host memory, dg_step(1), "
-                       "dg_get_state to host; host wall clock"}
+                       "dg_get_state to host; host wall clock; value from the total"}
 
     # ---- order sweep p = 1..4 (shorter runs, same mesh) ----
     sweep = {}
