@@ -513,8 +513,13 @@ def main():
                "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb,
                "steps": args.e2e_steps,
                "ms_per_step": {"min": per[0], "median": per[len(per) // 2], "max": per[-1]},
+               "value_at_median_step": K * N * npm * 3 / (per[len(per) // 2] / 1e3),
                "note": "per step: dg_set_state from pinned host memory, dg_step(1), "
-                       "dg_get_state to host; host wall clock; value from the total"}
+                       "dg_get_state to host; host wall clock; value from the total.  "
+                       "About every 0.48 s one host<->device copy of pinned memory "
+                       "stalls for 30-45 ms, plain torch copies alike (the host's "
+                       "doing, not the library's): the max, and the gap between the "
+                       "total and the median"}
 
     # ---- order sweep p = 1..4 (shorter runs, same mesh) ----
     sweep = {}
