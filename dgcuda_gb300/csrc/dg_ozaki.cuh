@@ -428,8 +428,10 @@ __device__ __forceinline__ void limit_epilogue(const Tab<P> &tab, const ElemArgs
   }
 }
 
-// 4 blocks per SM (128 registers) up to p = 3, where the extra warps hide
-// more latency than the spills cost; at p = 4 the shared memory holds 3
+// Blocks per SM: 5 at p = 2 (96 registers; its 32 KB of staging per block
+// leave room, and the extra warps hide more latency than the spills cost:
+// 5 % faster than 4, 6 blocks at 80 registers slower), 4 at p = 1 and 3 (128
+// registers; 48 KB of staging per block at p = 3), 3 at p = 4 (64 KB).
 // LIM: the limiter in the epilogue (the fused SSP-RK3 stage with the limiter
 // on): the output's means are a.M (k_means, from the same stage's side-flux
 // sums); each variable's new traces give its edge extremes, the means of the
@@ -437,7 +439,7 @@ __device__ __forceinline__ void limit_epilogue(const Tab<P> &tab, const ElemArgs
 // modes and traces -- limit_tr_body's rules -- are what is written; the
 // positivity rule is then applied to the limited traces (limit_epilogue).
 template <class Eq, int P, bool LIM = false>
-__global__ void __launch_bounds__(kOzThreads, P <= 3 ? 4 : 3) k_element_oz(const __grid_constant__ Tab<P> tab,
+__global__ void __launch_bounds__(kOzThreads, P == 2 ? 5 : P <= 3 ? 4 : 3) k_element_oz(const __grid_constant__ Tab<P> tab,
                                                            const __grid_constant__ EqP q,
                                                            const __grid_constant__ ElemArgs a,
                                                            const Tabs *__restrict__ ozt) {
