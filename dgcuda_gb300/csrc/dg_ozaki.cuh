@@ -263,7 +263,20 @@ __device__ __forceinline__ int quad_max(int m) {
 // not unrolled (one copy of each contraction in the code); what crosses
 // them -- area values, metric-folded fluxes, new traces -- is staged per
 // warp in shared memory, each lane in its own column.
-constexpr int kOzThreads = 128, kOzElems = 64;
+constexpr int kOzThreads = 128, kOzElems = 64;  // k_trace_oz: 4 warps of 16 elements
+
+// the element stage's block: warps (of 16 elements) per block and blocks per
+// SM, from its shared memory (GH doubles per lane) and registers.  5 warps
+// on an SM sub-partition leave 96 registers a thread (102 rounded down):
+// p = 2 runs 5 blocks of 4 warps there (32 KB of staging per block, 5 %
+// faster than 4 blocks at 128); p = 3 keeps 4 blocks at 128 (48 KB per
+// block; 6 blocks of 3 warps at 96 registers measured 26 % slower) and
+// p = 4 3 blocks at 168 (64 KB; 7 blocks of 2 warps at 128, 19 % slower).
+template <int P> struct OzBlock {
+  static constexpr int kWarps = 4;
+  static constexpr int kPerSM = P == 2 ? 5 : P == 4 ? 3 : 4;
+  static constexpr int kThreads = 32 * kWarps, kElems = 16 * kWarps;
+};
 
 template <class Eq, int P>
 struct OzShape {
@@ -276,7 +289,7 @@ struct OzShape {
   // a variable's g/h position PF, unused by its traces: where the fused
   // limiter keeps modes 1 and 2 of the unlimited output (p >= 2)
   static constexpr bool kStash = PF < 2 * PQ;
-  static constexpr size_t kSmem = (size_t)4 * GH * 32 * sizeof(double);
+  static constexpr size_t kSmem = (size_t)OzBlock<P>::kWarps * GH * 32 * sizeof(double);
 };
 
 // per-warp staging, one column per lane: slot k (0: g, 1: h) of variable n
@@ -428,10 +441,9 @@ __device__ __forceinline__ void limit_epilogue(const Tab<P> &tab, const ElemArgs
   }
 }
 
-// Blocks per SM: 5 at p = 2 (96 registers; its 32 KB of staging per block
-// leave room, and the extra warps hide more latency than the spills cost:
-// 5 % faster than 4, 6 blocks at 80 registers slower), 4 at p = 1 and 3 (128
-// registers; 48 KB of staging per block at p = 3), 3 at p = 4 (64 KB).
+// Blocks per SM (OzBlock): 5 at p = 2, where the extra warps hide more
+// latency than the spills at 96 registers cost (6 blocks at 80 registers
+// slower), 4 at p = 1 and 3, 3 at p = 4.
 // LIM: the limiter in the epilogue (the fused SSP-RK3 stage with the limiter
 // on): the output's means are a.M (k_means, from the same stage's side-flux
 // sums); each variable's new traces give its edge extremes, the means of the
@@ -439,7 +451,7 @@ __device__ __forceinline__ void limit_epilogue(const Tab<P> &tab, const ElemArgs
 // modes and traces -- limit_tr_body's rules -- are what is written; the
 // positivity rule is then applied to the limited traces (limit_epilogue).
 template <class Eq, int P, bool LIM = false>
-__global__ void __launch_bounds__(kOzThreads, P == 2 ? 5 : P <= 3 ? 4 : 3) k_element_oz(const __grid_constant__ Tab<P> tab,
+__global__ void __launch_bounds__(OzBlock<P>::kThreads, OzBlock<P>::kPerSM) k_element_oz(const __grid_constant__ Tab<P> tab,
                                                            const __grid_constant__ EqP q,
                                                            const __grid_constant__ ElemArgs a,
                                                            const Tabs *__restrict__ ozt) {
@@ -452,7 +464,7 @@ __global__ void __launch_bounds__(kOzThreads, P == 2 ? 5 : P <= 3 ? 4 : 3) k_ele
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, t = lane & 3;
   double *gh = smem_d + (size_t)warp * S::GH * 32;
   const int K = a.K, Kp = a.Kp;
-  const int e0 = (blockIdx.x * 4 + warp) * 16 + (lane >> 2);
+  const int e0 = (blockIdx.x * OzBlock<P>::kWarps + warp) * 16 + (lane >> 2);
   const int el[2] = {e0, e0 + 8};
   const bool live[2] = {el[0] < K, el[1] < K};
   const int ec[2] = {live[0] ? el[0] : K - 1, live[1] ? el[1] : K - 1};  // loads stay in bounds

@@ -12,14 +12,15 @@ namespace oz {
 
 template <int P>
 void euler_element(const Ctx &c, const ElemArgs &a, bool lim) {
-  const unsigned blocks = (unsigned)((c.m.K + kOzElems - 1) / kOzElems);
+  using B = OzBlock<P>;
+  const unsigned blocks = (unsigned)((c.m.K + B::kElems - 1) / B::kElems);
   const Tab<P> &tab = *reinterpret_cast<const Tab<P> *>(c.tab);
   const Tabs *t = static_cast<const Tabs *>(c.oz);
   if (lim)
-    k_element_oz<Euler, P, true><<<blocks, kOzThreads, oz_smem_bytes<Euler, P>(), c.st>>>(
+    k_element_oz<Euler, P, true><<<blocks, B::kThreads, oz_smem_bytes<Euler, P>(), c.st>>>(
         tab, *c.q, a, t);
   else
-    k_element_oz<Euler, P, false><<<blocks, kOzThreads, oz_smem_bytes<Euler, P>(), c.st>>>(
+    k_element_oz<Euler, P, false><<<blocks, B::kThreads, oz_smem_bytes<Euler, P>(), c.st>>>(
         tab, *c.q, a, t);
 }
 
