@@ -42,13 +42,15 @@ REF_CAP_S = 120.0  # the reference arm's timed steps stop after this many second
 
 def workload_config(n, p, steps_note):
     K = 2 * n * n
+    mb = K * 4 * (p + 1) * (p + 2) / 2 * 8 / 1e6
     return {
         "workload": "Euler four-quadrant Riemann, %dx%d squares -> %d triangles (jitter 0.1h, "
                     "seed 3), p=%d, Rusanov, SSP-RK3, Barth-Jespersen limiter, transmissive"
                     % (n, n, K, p),
         "equation": "euler", "p": p, "elements": K, "vars": 4, "modes": (p + 1) * (p + 2) // 2,
         "stages_per_step": 3, "cfl": 0.2, "precision": "fp64",
-        "l2": "no flush: state %.0f MB > 129 MB L2" % (K * 4 * (p + 1) * (p + 2) / 2 * 8 / 1e6),
+        "l2": ("no flush: state %.0f MB > 129 MB L2" % mb if mb > 129 else
+               "state %.0f MB fits the 129 MB L2 (a small case; no flush)" % mb),
         "parallelism": steps_note,
     }
 
