@@ -3,10 +3,13 @@
 Every CUDA translation unit is compiled for sm_103a only
 (``-gencode arch=compute_103a,code=sm_103a``); host C++ goes through nvcc as
 well so one toolchain links everything.  Objects land in ``_build/`` beside
-this file and are rebuilt when a source or any header is newer.  Translation
-units compile in parallel.
+this file and are rebuilt when a source or any header is newer, or when
+they were built on another host architecture or with other flags (a stamp
+in ``_build/``).  Translation units compile in parallel.
 """
+import hashlib
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -54,6 +57,25 @@ def _compile(src, flags):
     return obj
 
 
+def _check_stamp(flags):
+    """Drops objects and outputs built on another machine architecture or
+    with other flags: a newer mtime alone does not make them usable here."""
+    stamp = os.path.join(BUILD, "STAMP")
+    want = "%s %s" % (platform.machine(),
+                      hashlib.sha1(" ".join(ARCH + flags).encode()).hexdigest())
+    have = open(stamp).read().strip() if os.path.exists(stamp) else None
+    if have == want:
+        return
+    for f in os.listdir(BUILD):
+        if f.endswith(".o"):
+            os.remove(os.path.join(BUILD, f))
+    for f in (LIB, CLI):
+        if os.path.exists(f):
+            os.remove(f)
+    with open(stamp, "w") as fh:
+        fh.write(want + "\n")
+
+
 def build(verbose=False, jobs=None):
     os.makedirs(BUILD, exist_ok=True)
     # host code: no contraction of a*b+c into FMAs the source does not write,
@@ -62,6 +84,7 @@ def build(verbose=False, jobs=None):
               "-I" + CSRC,
               "-I" + os.path.join(ROOT, "include")]
     cuflags = common + ["-Xptxas", "-O3", "--expt-relaxed-constexpr"]
+    _check_stamp(cuflags)
     srcs = _sources()
     jobs = jobs or min(len(srcs), os.cpu_count() or 4)
     with ThreadPoolExecutor(jobs) as ex:
