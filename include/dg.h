@@ -276,8 +276,9 @@ dg_status dg_autotune_stage(dg_solver *s, int *block, int *threads_per_element);
  * Per RK stage one face launch covers every member (concatenated element
  * and side ranges; each member keeps its own mesh, order p in 1..3, CFL time
  * step and time) and the element stage is one launch per group of members
- * of one order and mesh-size class (dg_batch_autotune); one SSP-RK3 step of
- * the whole ensemble is one CUDA graph.  Members must share device, equation and limiter setting; they
+ * of one order and mesh-size class (dg_batch_autotune), the groups running
+ * concurrently; one SSP-RK3 step of the whole ensemble is one CUDA graph.
+ * Members must share device, equation and limiter setting; they
  * stay owned by the caller and must outlive the batch.  No reference
  * counterpart (DGCUDA runs one problem per process). */
 typedef struct dg_batch dg_batch;
